@@ -1,0 +1,222 @@
+/*
+ * mgldg.h -- C ABI of the GB300 (sm_103a) multigrid-preconditioned CG solver
+ * for LDG Poisson operators in block-sparse form.
+ *
+ * Drop-in for the solver path of danfortunato/multigrid-ldg.  The reference
+ * exposes that path as C++ templates; each entry point below names the
+ * reference interface it replaces (paths are relative to the reference tree).
+ *
+ *   SparseBlockMatrix<P,Q>      src/cartesian/util/sparseblockmatrix.h:62-165
+ *   multiply_*_mv*              src/cartesian/util/sparseblockmatrix.tpp:288-422
+ *   LDGOperators<N,P>           src/cartesian/dg/ldgpoisson.h:15-53
+ *   MG::Parameters              src/cartesian/multigrid/multigrid.h:48-62
+ *   Multigrid<N,P>              src/cartesian/multigrid/multigrid.h:280-433
+ *   pcg                         src/cartesian/multigrid/krylov.h:22-82
+ *
+ * Conventions
+ *  - Every call returns an int status (MGLDG_OK == 0).  The text of the last
+ *    error of a context is returned by mgldg_last_error().  No C++ exception
+ *    crosses this boundary.
+ *  - Blocks are dense row-major br x bc doubles; vectors are element-major
+ *    (dof = element * block_size + local node), the reference's layout.
+ *  - Arguments without a _dev suffix are host pointers; they are copied.
+ *    Functions with a _dev suffix take device pointers on the context's GPU
+ *    and run asynchronously on the context's stream.
+ *  - Handles own their device memory and free it in *_destroy.  A handle is
+ *    used by one host thread at a time; each context owns one CUDA stream.
+ */
+#ifndef MGLDG_H
+#define MGLDG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference's bool shape returns,
+ *      std::invalid_argument and asserts, mapped to codes) ---- */
+#define MGLDG_OK              0
+#define MGLDG_ERR_ARG         1  /* bad argument / unknown enum (multigrid.h:164,194,214) */
+#define MGLDG_ERR_SHAPE       2  /* block shapes do not conform (sparseblockmatrix.tpp:181-184) */
+#define MGLDG_ERR_CUDA        3  /* CUDA runtime failure */
+#define MGLDG_ERR_BREAKDOWN   4  /* PCG breakdown: d.q <= 0 or a non-finite scalar */
+#define MGLDG_ERR_TIMEOUT     5  /* a bounded device-side wait ran out */
+#define MGLDG_ERR_NOT_SPD     6  /* a block or the coarse matrix is singular / not SPD */
+#define MGLDG_ERR_NOMEM       7  /* device allocation failed */
+#define MGLDG_ERR_UNSUPPORTED 8  /* valid request this build does not implement */
+
+typedef struct mgldg_ctx mgldg_ctx;
+typedef struct mgldg_bsr mgldg_bsr;
+typedef struct mgldg_ops mgldg_ops;
+typedef struct mgldg_mg mgldg_mg;
+typedef struct mgldg_problem mgldg_problem;
+
+/* ------------------------------------------------------------ context -- */
+/* Creates a context on CUDA device `device` with its own stream. */
+int mgldg_ctx_create(int device, mgldg_ctx** ctx);
+int mgldg_ctx_destroy(mgldg_ctx* ctx);
+/* Text of the last error reported through this context ("" if none). */
+const char* mgldg_last_error(const mgldg_ctx* ctx);
+/* Waits for all work queued on the context's stream. */
+int mgldg_ctx_sync(mgldg_ctx* ctx);
+/* The context's stream (a cudaStream_t), for callers that pass _dev data. */
+void* mgldg_ctx_stream(mgldg_ctx* ctx);
+/* Reference-element tables (master.h:147-214): P = nodes per dimension,
+ * 1..6.  nodes[P], denom[P], mass/invmass/diff[P*P]; quad_x/quad_w[10]. */
+int mgldg_master_tables(int P, double* nodes, double* denom, double* mass,
+                        double* invmass, double* diff, double* quad_x, double* quad_w);
+
+/* ------------------------------------------- block-sparse matrix (BSR) -- */
+/* Replaces SparseBlockMatrix<P,Q> assembly (setBlock/addToBlock,
+ * sparseblockmatrix.h:113-125) by a block-CSR upload: nbr x nbc blocks of
+ * br x bc; row_ptr[nbr+1], col_idx[nnzb] (any order within a row; stored
+ * sorted), vals[nnzb*br*bc].  Duplicate (i,j) entries are summed, as
+ * addToBlock does. */
+int mgldg_bsr_create(mgldg_ctx* ctx, int nbr, int nbc, int br, int bc,
+                     const int* row_ptr, const int* col_idx, const double* vals,
+                     mgldg_bsr** A);
+int mgldg_bsr_destroy(mgldg_bsr* A);
+/* blockRows/blockCols/rowsPerBlock/colsPerBlock/nnzb (sparseblockmatrix.h:82-110) */
+int mgldg_bsr_info(const mgldg_bsr* A, int* nbr, int* nbc, int* br, int* bc,
+                   int64_t* nnzb);
+/* Sorted block-CSR download (the stored pattern and values). */
+int mgldg_bsr_download(mgldg_ctx* ctx, const mgldg_bsr* A, int* row_ptr,
+                       int* col_idx, double* vals);
+/* y := alpha*A*x + beta*y  (multiply_add_mv / multiply_mv,
+ * sparseblockmatrix.tpp:288-301,358-371).  Host vectors. */
+int mgldg_bsr_mv(mgldg_ctx* ctx, double alpha, const mgldg_bsr* A,
+                 const double* x, double beta, double* y);
+int mgldg_bsr_mv_dev(mgldg_ctx* ctx, double alpha, const mgldg_bsr* A,
+                     const double* x, double beta, double* y);
+/* y := A^T x  (multiply_mv_t, sparseblockmatrix.tpp:322-335).  Host vectors. */
+int mgldg_bsr_mv_t(mgldg_ctx* ctx, const mgldg_bsr* A, const double* x, double* y);
+
+/* ------------------------------------------------------ LDG operators -- */
+/* LDGOperators<N,P>{M, Minv, G[N], T, A} (ldgpoisson.h:15-31).  Takes
+ * ownership of M, G[0..ndim-1] and T (they are destroyed with ops). */
+int mgldg_ops_create(mgldg_ctx* ctx, int ndim, mgldg_bsr* M, mgldg_bsr* const* G,
+                     mgldg_bsr* T, mgldg_ops** ops);
+/* Operators holding only the Laplacian A (enough for RAT coarsening, for
+ * pcg and for Jacobi / Gauss-Seidel).  Takes ownership of A. */
+int mgldg_ops_create_A(mgldg_ctx* ctx, mgldg_bsr* A, mgldg_ops** ops);
+/* A = T + sum_d G_d^T M G_d  (construct_laplacian, ldgpoisson.h:34-52),
+ * symbolic product on the host, numeric product on the GPU. */
+int mgldg_ops_construct_laplacian(mgldg_ctx* ctx, mgldg_ops* ops);
+/* which: 0=M 1=G0 2=G1 3=T 4=A.  The handle stays owned by ops. */
+int mgldg_ops_get(const mgldg_ops* ops, int which, const mgldg_bsr** A);
+int mgldg_ops_destroy(mgldg_ops* ops);
+
+/* ---------------------------------------------------------- multigrid -- */
+#define MGLDG_RELAX_JACOBI       0   /* MG::kJacobi */
+#define MGLDG_RELAX_GAUSS_SEIDEL 1   /* MG::kGaussSeidel */
+#define MGLDG_COARSE_CHOLESKY    0   /* MG::kCholesky: one-element coarsest level */
+#define MGLDG_COARSE_RELAXATION  1   /* MG::kRelaxation */
+#define MGLDG_COARSE_DENSE       2   /* extension: dense Cholesky of a multi-element coarsest level */
+#define MGLDG_RESTRICT_RAT       0   /* MG::kRAT */
+#define MGLDG_RESTRICT_RATRAT    1   /* MG::kRATRAT */
+#define MGLDG_PREC_FP64          0   /* plain form: FP64 throughout */
+#define MGLDG_PREC_MIXED         1   /* FP32 V-cycle, FP64 coarsest solve (and FP64 pcg) */
+
+/* MG::Parameters (multigrid.h:48-62) plus the build's extensions. */
+typedef struct mgldg_mg_params {
+    int relaxation;     /* default MGLDG_RELAX_GAUSS_SEIDEL */
+    double omega;       /* default 0.8 */
+    int solver;         /* default MGLDG_COARSE_CHOLESKY */
+    int npre;           /* default 3 */
+    int npost;          /* default 3 */
+    int restriction;    /* default MGLDG_RESTRICT_RATRAT */
+    int precision;      /* default MGLDG_PREC_FP64 */
+    int max_levels;     /* 0: the whole hierarchy (reference); k: keep k levels */
+    int mean_project;   /* 1 (reference, multigrid.h:367): b -= mean(b) on the coarsest level */
+} mgldg_mg_params;
+
+void mgldg_mg_params_default(mgldg_mg_params* p);
+/* Multigrid<N,P>(ops, hierarchy, params) (multigrid.h:291-301, setup
+ * :404-411, Level constructors :83-171).  T[l] interpolates level l+1 to
+ * level l (InterpolationHierarchy<N,P>::T, interpolationhierarchy.h:91);
+ * its values are copied.  `fine` is borrowed and must outlive mg. */
+int mgldg_mg_create(mgldg_ctx* ctx, const mgldg_ops* fine, const mgldg_bsr* const* T,
+                    int nT, const mgldg_mg_params* params, mgldg_mg** mg);
+int mgldg_mg_destroy(mgldg_mg* mg);
+int mgldg_mg_nlevels(const mgldg_mg* mg, int* nlevels);
+/* Operators of level l (level(i)->ops, multigrid.h:352-355); which as in
+ * mgldg_ops_get.  Owned by mg. */
+int mgldg_mg_level_op(const mgldg_mg* mg, int level, int which, const mgldg_bsr** A);
+/* One V-cycle from level 0 (vcycle(), multigrid.h:361-383) on rhs b with
+ * initial guess / result x (solution(), rhs()). */
+int mgldg_mg_vcycle(mgldg_ctx* ctx, mgldg_mg* mg, const double* b, double* x);
+int mgldg_mg_vcycle_dev(mgldg_ctx* ctx, mgldg_mg* mg, const double* b, double* x);
+/* n relaxations on `level` (relax(n, reverse), multigrid.h:202-216). */
+int mgldg_mg_relax(mgldg_ctx* ctx, mgldg_mg* mg, int level, int n, int reverse,
+                   const double* b, double* x);
+
+/* ---------------------------------------------------------------- pcg -- */
+/* pcg(A, b, x, precon, tol, maxit) (krylov.h:22-68) with precon = one
+ * V-cycle from x = 0 (dg_tests.cpp:300-305); mg == NULL gives the
+ * unpreconditioned overload (krylov.h:78-82).  x is the initial guess and
+ * the result.  iters (may be NULL) receives the iteration count; res_hist
+ * (may be NULL, maxit doubles) receives ||r|| after each iteration, the
+ * value the reference prints.  Returns MGLDG_OK also when maxit is reached. */
+int mgldg_pcg(mgldg_ctx* ctx, mgldg_mg* mg, const mgldg_bsr* A, const double* b,
+              double* x, double tol, int maxit, int* iters, double* res_hist);
+int mgldg_pcg_dev(mgldg_ctx* ctx, mgldg_mg* mg, const mgldg_bsr* A, const double* b,
+                  double* x, double tol, int maxit, int* iters, double* res_hist);
+
+/* ------------------------------------- Cartesian problem builder ---------
+ * The callers on either side of the path, for users without the reference's
+ * assembly: a uniform quadtree mesh of n x n squares on [0,1]^2 (n a power
+ * of two), elements in the reference's depth-first order, Q_{P-1} nodal LDG
+ * with homogeneous Dirichlet data (LDGPoisson<2,P>, ldgpoisson.tpp:14-161,
+ * assembled on the GPU) and its h-interpolation hierarchy
+ * (interpolationhierarchy.h:30-82). */
+int mgldg_cartesian_create(mgldg_ctx* ctx, int P, int n, double tau0, double tauD,
+                           mgldg_problem** pr);
+int mgldg_problem_destroy(mgldg_problem* pr);
+int mgldg_problem_info(const mgldg_problem* pr, int* ne, int* npl, int64_t* ndof, int* nT);
+/* Borrowed handles, owned by pr. */
+int mgldg_problem_ops(mgldg_problem* pr, mgldg_ops** ops);
+int mgldg_problem_interp(mgldg_problem* pr, int l, const mgldg_bsr** T);
+/* b = M f with f the nodal interpolant of a sum of 8 Gaussians drawn from
+ * `seed` (centres U[0,1]^2, widths U[0.05,0.2], amplitudes N(0,1)).
+ * _dev writes a device vector. */
+int mgldg_problem_rhs_gaussian(mgldg_ctx* ctx, mgldg_problem* pr, uint64_t seed, double* b);
+int mgldg_problem_rhs_gaussian_dev(mgldg_ctx* ctx, mgldg_problem* pr, uint64_t seed, double* b);
+
+/* ------------------------------------------------------------ host logic -- */
+/* Level sets of the block Gauss-Seidel sweep (host only, no GPU needed): for
+ * the forward sweep of multigrid.h:240-249 (reverse=0) or the reverse sweep
+ * of :251-261 (reverse=1), level[i] = 1 + max level of the rows that precede
+ * row i in sweep order and share a block with it.  order[] lists the rows by
+ * level; nlevels is the number of dependent steps of one sweep. */
+int mgldg_gs_levels(int nbr, const int* row_ptr, const int* col_idx, int reverse,
+                    int* level, int* order, int* nlevels);
+/* Failure-detection self test (no reference counterpart): runs the
+ * Gauss-Seidel kernel on a two-row system whose dependency is never
+ * released, so its bounded wait expires after timeout_ns.  *status receives
+ * MGLDG_ERR_TIMEOUT when the kernel reported the expiry; the call itself
+ * returns MGLDG_OK when the context stayed usable. */
+int mgldg_selftest_wait_timeout(mgldg_ctx* ctx, int64_t timeout_ns, int* status);
+
+/* ------------------------------------------------------------ profiling -- */
+#define MGLDG_K_SPMV      0   /* BSR SpMV / residual (FP64 or FP32) */
+#define MGLDG_K_GS        1   /* level-scheduled block Gauss-Seidel sweep */
+#define MGLDG_K_JACOBI    2   /* fused block-Jacobi sweep */
+#define MGLDG_K_TRANSFER  3   /* restriction / prolongation */
+#define MGLDG_K_COARSE    4   /* coarsest-level solve */
+#define MGLDG_K_VECTOR    5   /* pcg dots / axpys / conversions */
+#define MGLDG_K_SETUP     6   /* assembly, Galerkin products, block inverses */
+#define MGLDG_K_NCLASS    7
+/* on=1: time every kernel launch with CUDA events on the context's stream. */
+int mgldg_prof_enable(mgldg_ctx* ctx, int on);
+int mgldg_prof_reset(mgldg_ctx* ctx);
+/* Launch count and summed event time (ms) of one kernel class since reset
+ * (time only while enabled).  Synchronises the stream. */
+int mgldg_prof_query(mgldg_ctx* ctx, int kclass, int64_t* launches, double* ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MGLDG_H */

@@ -1,0 +1,563 @@
+// cartesian.cu -- the callers on either side of the solver path for a
+// uniform Cartesian quadtree: mesh topology, LDG operator assembly on the
+// GPU, the h-interpolation hierarchy and the Gaussian-sum right-hand side.
+//
+// Reference: Quadtree / Mesh (src/cartesian/mesh/quadtree.tpp:10-127,
+// mesh.h:186-352), LDGPoisson::discretize (src/cartesian/dg/ldgpoisson.tpp:
+// 14-100), computeRHS (:167-176) and InterpolationHierarchy
+// (src/cartesian/multigrid/interpolationhierarchy.h:30-82).
+//
+// Elements are numbered in the reference's depth-first quadtree order, which
+// on a uniform 2^L x 2^L tree is the Morton order with the x bit above the y
+// bit at every level.  All blocks of the LDG operators on a uniform mesh are
+// sums of a few distinct contributions (mass, broken gradient, lifting and
+// penalty terms per face orientation); the host builds that short table with
+// the reference's arithmetic, and for every stored block the ordered list of
+// contributions in the reference's face order.  The GPU then writes every
+// block (the bulk of the work: bytes), one thread per block entry.
+#include <algorithm>
+#include <cmath>
+#include <random>
+
+#include "api.cuh"
+#include "master_tables.inc"
+
+using namespace mg;
+
+namespace mg {
+
+typedef std::vector<double> Blk;   // row-major b x b
+
+struct Gauss8 {
+    double cx[8], cy[8], w[8], a[8];
+};
+
+// 8 Gaussians: centres U[0,1]^2, widths U[0.05,0.2], amplitudes N(0,1);
+// mt19937_64, 53-bit uniforms, Box-Muller with the cosine branch
+static Gauss8 gaussian_params(uint64_t seed) {
+    std::mt19937_64 g(seed);
+    auto uni = [&]() { return (double)(g() >> 11) * 0x1.0p-53; };
+    Gauss8 p;
+    for (int k = 0; k < 8; ++k) {
+        p.cx[k] = uni();
+        p.cy[k] = uni();
+        p.w[k] = 0.05 + 0.15 * uni();
+        double u1;
+        do { u1 = uni(); } while (u1 <= 0.0);
+        double u2 = uni();
+        p.a[k] = std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * 3.14159265358979323846 * u2);
+    }
+    return p;
+}
+
+static uint32_t morton_encode(uint32_t ix, uint32_t iy) {
+    uint32_t e = 0;
+    for (int bit = 0; bit < 16; ++bit) {
+        e |= ((ix >> bit) & 1u) << (2 * bit + 1);
+        e |= ((iy >> bit) & 1u) << (2 * bit);
+    }
+    return e;
+}
+static void morton_decode(uint32_t e, uint32_t& ix, uint32_t& iy) {
+    ix = iy = 0;
+    for (int bit = 0; bit < 16; ++bit) {
+        ix |= ((e >> (2 * bit + 1)) & 1u) << bit;
+        iy |= ((e >> (2 * bit)) & 1u) << bit;
+    }
+}
+
+struct Ref2 {
+    int P, b;
+    const double* nodes;
+    const double* denom;
+    const double* mass1;
+    const double* invmass1;
+    const double* diff1;
+    explicit Ref2(int P_) : P(P_), b(P_ * P_) {
+        nodes = kNodes[P - 1]; denom = kDenom[P - 1];
+        mass1 = kMass1[P - 1]; invmass1 = kInvMass1[P - 1]; diff1 = kDiff1[P - 1];
+    }
+    // tensorProduct<2,P> (master.h:121-135)
+    Blk tensor(const double* A) const {
+        Blk M((size_t)b * b);
+        for (int i0 = 0; i0 < P; ++i0)
+            for (int i1 = 0; i1 < P; ++i1)
+                for (int j0 = 0; j0 < P; ++j0)
+                    for (int j1 = 0; j1 < P; ++j1) {
+                        double v = 1.0;
+                        v *= A[i0 * P + j0];
+                        v *= A[i1 * P + j1];
+                        M[(size_t)(i0 * P + i1) * b + j0 * P + j1] = v;
+                    }
+        return M;
+    }
+    // Master<2,P>::diff(dim) (master.h:45-68)
+    Blk diff(int dim) const {
+        Blk D((size_t)b * b, 0.0);
+        for (int i0 = 0; i0 < P; ++i0)
+            for (int i1 = 0; i1 < P; ++i1)
+                for (int j0 = 0; j0 < P; ++j0)
+                    for (int j1 = 0; j1 < P; ++j1) {
+                        int it[2] = {i0, i1}, jt[2] = {j0, j1};
+                        if (it[1 - dim] != jt[1 - dim]) continue;
+                        D[(size_t)(i0 * P + i1) * b + j0 * P + j1] = diff1[it[dim] * P + jt[dim]];
+                    }
+        return D;
+    }
+    // LagrangePoly<P>::eval (master.h:79-94)
+    void lagrange1(double x, double* l) const {
+        double alpha = 1;
+        l[0] = denom[0];
+        for (int i = 0; i < P - 1; ++i) {
+            alpha *= x - nodes[i];
+            l[i + 1] = alpha * denom[i + 1];
+        }
+        double beta = 1;
+        for (int i = P - 1; i > 0; --i) {
+            beta *= x - nodes[i];
+            l[i - 1] *= beta;
+        }
+    }
+    void lagrange2(const double* x, double* out) const {
+        double g0[8], g1[8];
+        lagrange1(x[0], g0);
+        lagrange1(x[1], g1);
+        for (int i0 = 0; i0 < P; ++i0)
+            for (int i1 = 0; i1 < P; ++i1) {
+                double v = 1;
+                v *= g0[i0];
+                v *= g1[i1];
+                out[i0 * P + i1] = v;
+            }
+    }
+};
+
+static Blk bscale(double s, const Blk& A) {
+    Blk C(A.size());
+    for (size_t k = 0; k < A.size(); ++k) C[k] = s * A[k];
+    return C;
+}
+static Blk bmul(const Blk& A, const Blk& B, int b) {
+    Blk C((size_t)b * b);
+    for (int i = 0; i < b; ++i)
+        for (int j = 0; j < b; ++j) {
+            double s = 0;
+            for (int k = 0; k < b; ++k) s += A[(size_t)i * b + k] * B[(size_t)k * b + j];
+            C[(size_t)i * b + j] = s;
+        }
+    return C;
+}
+static Blk btrans(const Blk& A, int b) {
+    Blk C(A.size());
+    for (int i = 0; i < b; ++i)
+        for (int j = 0; j < b; ++j) C[(size_t)j * b + i] = A[(size_t)i * b + j];
+    return C;
+}
+
+// out block o = sum of table[tidx[t]], t in [tptr[o], tptr[o+1]) in order
+__global__ void k_sum_blocks(int64_t nout, int bsz, const int64_t* __restrict__ tptr, const int* __restrict__ tidx,
+                             const double* __restrict__ table, double* __restrict__ out) {
+    for (int64_t t = (int64_t)blockIdx.x * 256 + threadIdx.x; t < nout * bsz; t += (int64_t)gridDim.x * 256) {
+        const int64_t o = t / bsz;
+        const int e = (int)(t - o * bsz);
+        double v = 0.0;
+        const int64_t t0 = tptr[o], t1 = tptr[o + 1];
+        if (t1 > t0) v = table[(size_t)tidx[t0] * bsz + e];
+        for (int64_t q = t0 + 1; q < t1; ++q) v += table[(size_t)tidx[q] * bsz + e];
+        out[t] = v;
+    }
+}
+
+// b_e = M_e f_e with f the Gaussian sum at the element's Gauss-Lobatto nodes
+struct GaussDev {
+    double cx[8], cy[8], w[8], a[8];
+};
+__global__ void k_rhs_gaussian(int ne, int P, int n, double h, GaussDev g, const double* __restrict__ nodes,
+                               const double* __restrict__ Mblk, double* __restrict__ out) {
+    extern __shared__ double sf[];
+    const int b = P * P;
+    for (int e = blockIdx.x; e < ne; e += gridDim.x) {
+        uint32_t ix = 0, iy = 0;
+        for (int bit = 0; bit < 16; ++bit) {
+            ix |= (((uint32_t)e >> (2 * bit + 1)) & 1u) << bit;
+            iy |= (((uint32_t)e >> (2 * bit)) & 1u) << bit;
+        }
+        const double lox = ix * h, loy = iy * h;
+        for (int q = threadIdx.x; q < b; q += blockDim.x) {
+            const int i0 = q / P, i1 = q - i0 * P;
+            const double x = lox + h * nodes[i0], y = loy + h * nodes[i1];
+            double s = 0;
+            for (int k = 0; k < 8; ++k) {
+                const double dx = x - g.cx[k], dy = y - g.cy[k];
+                s += g.a[k] * exp(-(dx * dx + dy * dy) / (2.0 * g.w[k] * g.w[k]));
+            }
+            sf[q] = s;
+        }
+        __syncthreads();
+        for (int r = threadIdx.x; r < b; r += blockDim.x) {
+            double s = 0;
+            for (int c = 0; c < b; ++c) s += Mblk[r * b + c] * sf[c];
+            out[(size_t)e * b + r] = s;
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace mg
+
+struct mgldg_problem {
+    mgldg_ctx* ctx = nullptr;
+    int P = 0, b = 0, n = 0, ne = 0;
+    double h = 0;
+    mgldg_ops* ops = nullptr;
+    std::vector<mgldg_bsr*> T;
+    double* d_nodes = nullptr;
+    double* d_M = nullptr;
+    ~mgldg_problem() {
+        delete ops;
+        for (auto* t : T) delete t;
+        dfree(d_nodes);
+        dfree(d_M);
+    }
+};
+
+namespace mg {
+
+// builds one operator from per-block contribution lists
+struct Assembly {
+    std::vector<int> row_ptr, col_idx;
+    std::vector<int64_t> tptr{0};
+    std::vector<int> tidx;
+    void begin_row() {}
+    void add_block(int col, std::initializer_list<int> contrib) {
+        col_idx.push_back(col);
+        for (int c : contrib) tidx.push_back(c);
+        tptr.push_back((int64_t)tidx.size());
+    }
+    void add_block_v(int col, const std::vector<int>& contrib) {
+        col_idx.push_back(col);
+        for (int c : contrib) tidx.push_back(c);
+        tptr.push_back((int64_t)tidx.size());
+    }
+};
+
+static mgldg_bsr* realize(mgldg_ctx* ctx, const Assembly& As, int ne, int b, const double* d_table) {
+    mgldg_bsr* A = bsr_new(ctx, ne, ne, b, b, As.row_ptr, As.col_idx);
+    int64_t* dptr = nullptr;
+    int* didx = nullptr;
+    try {
+        dptr = dalloc<int64_t>(As.tptr.size());
+        didx = dalloc<int>(std::max<size_t>(1, As.tidx.size()));
+        upload(ctx, dptr, As.tptr.data(), As.tptr.size());
+        upload(ctx, didx, As.tidx.data(), As.tidx.size());
+        const int64_t nout = (int64_t)As.col_idx.size();
+        const int bsz = b * b;
+        int g = (int)std::min<int64_t>((nout * bsz + 255) / 256, ctx->sm_count * 64);
+        {
+            Launch L(ctx, MGLDG_K_SETUP);
+            k_sum_blocks<<<std::max(1, g), 256, 0, ctx->stream>>>(nout, bsz, dptr, didx, d_table, A->val);
+        }
+        check_launch();
+        sync(ctx);
+    } catch (...) {
+        dfree(dptr);
+        dfree(didx);
+        delete A;
+        throw;
+    }
+    dfree(dptr);
+    dfree(didx);
+    return A;
+}
+
+static mgldg_problem* cartesian_create(mgldg_ctx* ctx, int P, int n, double tau0, double tauD) {
+    MG_REQUIRE(P >= 1 && P <= 5, MGLDG_ERR_UNSUPPORTED, "P must be 1..5 (block size <= 25)");
+    MG_REQUIRE(n >= 1 && n <= 32768 && (n & (n - 1)) == 0, MGLDG_ERR_ARG, "n must be a power of two");
+    const Ref2 R(P);
+    const int b = R.b;
+    const int ne = n * n;
+    const double h = 1.0 / n;
+    const double area = h, vol = h * h;
+
+    // ---- distinct contributions (the reference's per-face arithmetic) ----
+    Blk Mblk = bscale(vol, R.tensor(R.mass1));
+    Blk Minv = bscale(1 / vol, R.tensor(R.invmass1));
+    std::vector<Blk> table;
+    auto add = [&](Blk&& B) { table.push_back(std::move(B)); return (int)table.size() - 1; };
+    const int cM = add(Blk(Mblk));
+    int cDg[2], cGRR[2], cGRL[2], cGB[2][2], cTRR[2], cTLL[2], cTRL[2], cTLR[2], cTB[2][2];
+    for (int d = 0; d < 2; ++d) {
+        double jac = 1.0 / h;
+        cDg[d] = add(bscale(jac, R.diff(d)));
+        // canonical interior face in dimension d (mesh.h:285-310)
+        Blk LL((size_t)b * b, 0.0), RR((size_t)b * b, 0.0), RL((size_t)b * b, 0.0);
+        int jl[8], jr[8];
+        for (int a = 0; a < P; ++a) {
+            int jt[2];
+            jt[1 - d] = a;
+            jt[d] = P - 1;
+            jl[a] = jt[0] * P + jt[1];
+            jt[d] = 0;
+            jr[a] = jt[0] * P + jt[1];
+        }
+        for (int a = 0; a < P; ++a)
+            for (int c = 0; c < P; ++c) {
+                double m = R.mass1[a * P + c] * area;
+                LL[(size_t)jl[a] * b + jl[c]] = m;
+                RR[(size_t)jr[a] * b + jr[c]] = m;
+                RL[(size_t)jr[a] * b + jl[c]] = m;
+            }
+        cGRR[d] = add(bmul(bscale(1.0, Minv), RR, b));
+        cGRL[d] = add(bmul(bscale(-1.0, Minv), RL, b));
+        cTRR[d] = add(bscale(tau0, RR));
+        cTLL[d] = add(bscale(tau0, LL));
+        cTRL[d] = add(bscale(-tau0, RL));
+        cTLR[d] = add(bscale(-tau0, btrans(RL, b)));
+        // boundary faces of dimension d, side s (0: lower, normal -1; 1:
+        // upper, normal +1): 10-point Gauss rule (mesh.h:312-351)
+        for (int sd = 0; sd < 2; ++sd) {
+            const double nrm = sd ? 1.0 : -1.0;
+            std::vector<double> phi((size_t)MGLDG_QF * b), w(MGLDG_QF);
+            for (int q = 0; q < MGLDG_QF; ++q) {
+                double ql[2];
+                ql[1 - d] = kQuadNodes[q];
+                ql[d] = (nrm > 0) ? 1 : 0;
+                R.lagrange2(ql, &phi[(size_t)q * b]);
+                w[q] = 1;
+                w[q] *= kQuadWeights[q];
+            }
+            for (int q = 0; q < MGLDG_QF; ++q) w[q] *= area;
+            Blk Lm((size_t)b * MGLDG_QF);
+            for (int a = 0; a < b; ++a)
+                for (int q = 0; q < MGLDG_QF; ++q) Lm[(size_t)a * MGLDG_QF + q] = phi[(size_t)q * b + a] * w[q];
+            Blk LLb((size_t)b * b);
+            for (int a = 0; a < b; ++a)
+                for (int c = 0; c < b; ++c) {
+                    double s = 0;
+                    for (int q = 0; q < MGLDG_QF; ++q) s += Lm[(size_t)a * MGLDG_QF + q] * phi[(size_t)q * b + c];
+                    LLb[(size_t)a * b + c] = s;
+                }
+            cGB[d][sd] = add(bmul(bscale(-nrm, Minv), LLb, b));
+            cTB[d][sd] = add(bscale(tauD, LLb));
+        }
+    }
+
+    // ---- per-block contribution lists in the reference's face order ----
+    Assembly AM, AG[2], AT;
+    AM.row_ptr.push_back(0);
+    AG[0].row_ptr.push_back(0);
+    AG[1].row_ptr.push_back(0);
+    AT.row_ptr.push_back(0);
+    for (int e = 0; e < ne; ++e) {
+        uint32_t ix, iy;
+        morton_decode((uint32_t)e, ix, iy);
+        const uint32_t c[2] = {ix, iy};
+        int left[2], right[2];
+        for (int d = 0; d < 2; ++d) {
+            uint32_t lx = ix, ly = iy, rx = ix, ry = iy;
+            if (d == 0) { lx = ix - 1; rx = ix + 1; } else { ly = iy - 1; ry = iy + 1; }
+            left[d] = (c[d] > 0) ? (int)morton_encode(lx, ly) : -1;
+            right[d] = (c[d] + 1 < (uint32_t)n) ? (int)morton_encode(rx, ry) : -1;
+        }
+        // mass
+        AM.add_block(e, {cM});
+        AM.row_ptr.push_back((int)AM.col_idx.size());
+        // gradients: G_d(e,left) and G_d(e,e)
+        for (int d = 0; d < 2; ++d) {
+            std::vector<int> diag{cDg[d]};
+            if (left[d] >= 0) diag.push_back(cGRR[d]);
+            if (left[d] < 0) diag.push_back(cGB[d][0]);
+            if (right[d] < 0) diag.push_back(cGB[d][1]);
+            if (left[d] >= 0) AG[d].add_block(left[d], {cGRL[d]});   // left < e in Morton order
+            AG[d].add_block_v(e, diag);
+            AG[d].row_ptr.push_back((int)AG[d].col_idx.size());
+        }
+        // penalty: faces where e is the right element come first, in the
+        // order of their left elements; then e's own faces in (dim, dir)
+        std::vector<int> tdiag;
+        {
+            int l0 = left[0], l1 = left[1];
+            if (l0 >= 0 && l1 >= 0) {
+                if (l0 < l1) { tdiag.push_back(cTRR[0]); tdiag.push_back(cTRR[1]); }
+                else { tdiag.push_back(cTRR[1]); tdiag.push_back(cTRR[0]); }
+            } else if (l0 >= 0) {
+                tdiag.push_back(cTRR[0]);
+            } else if (l1 >= 0) {
+                tdiag.push_back(cTRR[1]);
+            }
+            for (int d = 0; d < 2; ++d) {
+                if (left[d] < 0) tdiag.push_back(cTB[d][0]);
+                if (right[d] < 0) tdiag.push_back(cTB[d][1]);
+                else tdiag.push_back(cTLL[d]);
+            }
+        }
+        struct Ent { int col; std::vector<int> c; };
+        std::vector<Ent> row;
+        for (int d = 0; d < 2; ++d) {
+            if (left[d] >= 0) row.push_back({left[d], {cTRL[d]}});
+            if (right[d] >= 0) row.push_back({right[d], {cTLR[d]}});
+        }
+        row.push_back({e, tdiag});
+        std::sort(row.begin(), row.end(), [](const Ent& a, const Ent& b2) { return a.col < b2.col; });
+        for (auto& en : row) AT.add_block_v(en.col, en.c);
+        AT.row_ptr.push_back((int)AT.col_idx.size());
+    }
+
+    mgldg_problem* pr = new mgldg_problem();
+    pr->ctx = ctx;
+    pr->P = P; pr->b = b; pr->n = n; pr->ne = ne; pr->h = h;
+    double* d_table = nullptr;
+    mgldg_bsr *M = nullptr, *G0 = nullptr, *G1 = nullptr, *Tm = nullptr;
+    try {
+        std::vector<double> flat;
+        for (auto& B : table) flat.insert(flat.end(), B.begin(), B.end());
+        d_table = dalloc<double>(flat.size());
+        upload(ctx, d_table, flat.data(), flat.size());
+        M = realize(ctx, AM, ne, b, d_table);
+        G0 = realize(ctx, AG[0], ne, b, d_table);
+        G1 = realize(ctx, AG[1], ne, b, d_table);
+        Tm = realize(ctx, AT, ne, b, d_table);
+        pr->ops = new mgldg_ops();
+        pr->ops->ctx = ctx;
+        pr->ops->ndim = 2;
+        pr->ops->M = M; M = nullptr;
+        pr->ops->G[0] = G0; G0 = nullptr;
+        pr->ops->G[1] = G1; G1 = nullptr;
+        pr->ops->T = Tm; Tm = nullptr;
+        construct_laplacian(ctx, pr->ops);
+        pr->d_nodes = dalloc<double>(P);
+        upload(ctx, pr->d_nodes, R.nodes, P);
+        pr->d_M = dalloc<double>((size_t)b * b);
+        upload(ctx, pr->d_M, Mblk.data(), Mblk.size());
+
+        // ---- h-interpolation hierarchy (interpolationhierarchy.h:30-82) ----
+        // fine element k of level l lies in parent k>>2 at child position
+        // k&3 = (x bit, y bit); its block evaluates the parent's Lagrange
+        // basis at the child's nodes.  Four distinct blocks per level.
+        std::vector<double> E4((size_t)4 * b * b);
+        for (int cpos = 0; cpos < 4; ++cpos) {
+            const double lo[2] = {0.5 * (cpos >> 1), 0.5 * (cpos & 1)};
+            for (int i0 = 0; i0 < P; ++i0)
+                for (int i1 = 0; i1 < P; ++i1) {
+                    double node[2];
+                    int idx[2] = {i0, i1};
+                    for (int d = 0; d < 2; ++d) node[d] = lo[d] + 0.5 * R.nodes[idx[d]];
+                    R.lagrange2(node, &E4[(size_t)cpos * b * b + (size_t)(i0 * P + i1) * b]);
+                }
+        }
+        for (int nf = n; nf > 1; nf >>= 1) {
+            const int nef = nf * nf, nec = nef / 4;
+            std::vector<int> rp(nef + 1), ci(nef);
+            mgldg_bsr* Tl = new mgldg_bsr();
+            pr->T.push_back(Tl);
+            Tl->ctx = ctx;
+            Tl->nbr = nef; Tl->nbc = nec; Tl->br = b; Tl->bc = b;
+            Tl->nnzb = nef; Tl->nuniq = 4;
+            Tl->h_blk.resize(nef);
+            for (int k = 0; k < nef; ++k) {
+                rp[k] = k;
+                ci[k] = k >> 2;
+                Tl->h_blk[k] = k & 3;
+            }
+            rp[nef] = nef;
+            Tl->h_row_ptr = rp;
+            Tl->h_col_idx = ci;
+            Tl->row_ptr = dalloc<int>(nef + 1);
+            Tl->col_idx = dalloc<int>(nef);
+            Tl->blk = dalloc<int>(nef);
+            Tl->val = dalloc<double>(E4.size());
+            upload(ctx, Tl->row_ptr, rp.data(), rp.size());
+            upload(ctx, Tl->col_idx, ci.data(), ci.size());
+            upload(ctx, Tl->blk, Tl->h_blk.data(), nef);
+            upload(ctx, Tl->val, E4.data(), E4.size());
+            (void)nec;
+        }
+        sync(ctx);
+    } catch (...) {
+        dfree(d_table);
+        delete M; delete G0; delete G1; delete Tm;
+        delete pr;
+        throw;
+    }
+    dfree(d_table);
+    return pr;
+}
+
+static void rhs_gaussian_dev(mgldg_ctx* ctx, mgldg_problem* pr, uint64_t seed, double* b) {
+    Gauss8 g = gaussian_params(seed);
+    GaussDev gd;
+    std::memcpy(gd.cx, g.cx, sizeof g.cx);
+    std::memcpy(gd.cy, g.cy, sizeof g.cy);
+    std::memcpy(gd.w, g.w, sizeof g.w);
+    std::memcpy(gd.a, g.a, sizeof g.a);
+    int grid = std::min(pr->ne, ctx->sm_count * 32);
+    {
+        Launch L(ctx, MGLDG_K_SETUP);
+        k_rhs_gaussian<<<grid, 128, pr->b * sizeof(double), ctx->stream>>>(pr->ne, pr->P, pr->n, pr->h, gd, pr->d_nodes,
+                                                                           pr->d_M, b);
+    }
+    check_launch();
+}
+
+}  // namespace mg
+
+// ================================================================== C ABI ==
+extern "C" int mgldg_cartesian_create(mgldg_ctx* ctx, int P, int n, double tau0, double tauD, mgldg_problem** out) {
+    MG_API_BEGIN(ctx)
+    MG_REQUIRE(out != nullptr, MGLDG_ERR_ARG, "null output");
+    *out = nullptr;
+    *out = cartesian_create(ctx, P, n, tau0, tauD);
+    MG_API_END
+}
+
+extern "C" int mgldg_problem_destroy(mgldg_problem* pr) {
+    if (!pr) return MGLDG_OK;
+    if (pr->ctx) cudaSetDevice(pr->ctx->device);
+    delete pr;
+    return MGLDG_OK;
+}
+
+extern "C" int mgldg_problem_info(const mgldg_problem* pr, int* ne, int* npl, int64_t* ndof, int* nT) {
+    if (!pr) return MGLDG_ERR_ARG;
+    if (ne) *ne = pr->ne;
+    if (npl) *npl = pr->b;
+    if (ndof) *ndof = (int64_t)pr->ne * pr->b;
+    if (nT) *nT = (int)pr->T.size();
+    return MGLDG_OK;
+}
+
+extern "C" int mgldg_problem_ops(mgldg_problem* pr, mgldg_ops** ops) {
+    if (!pr || !ops) return MGLDG_ERR_ARG;
+    *ops = pr->ops;
+    return MGLDG_OK;
+}
+
+extern "C" int mgldg_problem_interp(mgldg_problem* pr, int l, const mgldg_bsr** T) {
+    if (!pr || !T || l < 0 || l >= (int)pr->T.size()) return MGLDG_ERR_ARG;
+    *T = pr->T[l];
+    return MGLDG_OK;
+}
+
+extern "C" int mgldg_problem_rhs_gaussian_dev(mgldg_ctx* ctx, mgldg_problem* pr, uint64_t seed, double* b) {
+    MG_API_BEGIN(ctx)
+    MG_REQUIRE(pr && b, MGLDG_ERR_ARG, "null argument");
+    rhs_gaussian_dev(ctx, pr, seed, b);
+    MG_API_END
+}
+
+extern "C" int mgldg_problem_rhs_gaussian(mgldg_ctx* ctx, mgldg_problem* pr, uint64_t seed, double* b) {
+    MG_API_BEGIN(ctx)
+    MG_REQUIRE(pr && b, MGLDG_ERR_ARG, "null argument");
+    const int64_t n = (int64_t)pr->ne * pr->b;
+    double* d = dalloc<double>(n);
+    try {
+        rhs_gaussian_dev(ctx, pr, seed, d);
+        download(ctx, b, d, n);
+        sync(ctx);
+    } catch (...) {
+        dfree(d);
+        throw;
+    }
+    dfree(d);
+    MG_API_END
+}

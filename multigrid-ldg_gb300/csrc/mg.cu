@@ -1,0 +1,715 @@
+// mg.cu -- multigrid hierarchy, V-cycle and preconditioned CG.
+//
+// Reference: Multigrid<N,P> (src/cartesian/multigrid/multigrid.h:280-433),
+// its Level constructors (:83-171), relax/solve (:181-216), vcycle
+// (:361-383), restrict/correct (:414-425); pcg (krylov.h:22-82) and the
+// preconditioner closure of tests/cartesian/dg_tests.cpp:300-305.
+//
+// Precision forms: MGLDG_PREC_FP64 runs everything in FP64.  MGLDG_PREC_MIXED
+// keeps FP32 copies of every level operator, inverse diagonal block and
+// transfer, runs the whole V-cycle in FP32 with FP32 accumulation, and keeps
+// the coarsest solve (mean projection and dense inverse), the outer CG
+// residuals, dot products and updates in FP64.
+#include <algorithm>
+#include <cmath>
+
+#include "api.cuh"
+#include "smooth.cuh"
+
+using namespace mg;
+
+namespace mg {
+
+struct LevelData {
+    mgldg_ops* ops = nullptr;    // owned for coarse levels
+    bool owns_ops = false;
+    const mgldg_bsr* A = nullptr;
+    int ne = 0, b = 0;
+    int64_t n = 0;
+    double* Dinv = nullptr;
+    float* Dinv32 = nullptr;
+    Sched sched;
+    bool has_sched = false;
+    double *x = nullptr, *bb = nullptr, *r = nullptr, *xt = nullptr;
+    float *x32 = nullptr, *b32 = nullptr, *r32 = nullptr, *xt32 = nullptr;
+    mgldg_bsr* T = nullptr;    // interpolation to this level from the next coarser one
+    mgldg_bsr* Tt = nullptr;   // its transpose (restriction)
+};
+
+template <class T>
+struct LV;
+template <>
+struct LV<double> {
+    static double*& x(LevelData& L) { return L.x; }
+    static double*& b(LevelData& L) { return L.bb; }
+    static double*& r(LevelData& L) { return L.r; }
+    static double*& xt(LevelData& L) { return L.xt; }
+    static const double* D(LevelData& L) { return L.Dinv; }
+};
+template <>
+struct LV<float> {
+    static float*& x(LevelData& L) { return L.x32; }
+    static float*& b(LevelData& L) { return L.b32; }
+    static float*& r(LevelData& L) { return L.r32; }
+    static float*& xt(LevelData& L) { return L.xt32; }
+    static const float* D(LevelData& L) { return L.Dinv32; }
+};
+
+struct PcgScalars {
+    double delta_new, delta_old, delta0, alpha, beta, dq, rr, pad;
+    int breakdown, pad2[3];
+};
+
+}  // namespace mg
+
+struct mgldg_mg {
+    mgldg_ctx* ctx = nullptr;
+    mgldg_mg_params p;
+    std::vector<mg::LevelData> L;
+    double* Cinv = nullptr;   // dense inverse of the coarsest matrix
+    int nc = 0;
+    // pcg work space
+    double *r = nullptr, *d = nullptr, *q = nullptr, *s = nullptr, *hist = nullptr;
+    int64_t pcg_n = 0;
+    int pcg_maxit = 0;
+    mg::PcgScalars* sc = nullptr;
+    mg::PcgScalars* h_sc = nullptr;   // pinned
+    ~mgldg_mg();
+};
+
+namespace mg {
+
+// ------------------------------------------------------------- small kernels
+template <class A, class B>
+__global__ void k_convert(int64_t n, const A* __restrict__ a, B* __restrict__ b) {
+    for (int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (int64_t)gridDim.x * 256) b[i] = (B)a[i];
+}
+
+template <class A, class B>
+static void convert(mgldg_ctx* ctx, int64_t n, const A* a, B* b) {
+    if (n == 0) return;
+    int g = (int)std::min<int64_t>((n + 255) / 256, ctx->sm_count * 16);
+    {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_convert<A, B><<<g, 256, 0, ctx->stream>>>(n, a, b);
+    }
+    check_launch();
+}
+
+// coarsest level: b -= mean(b) (optional); x = Cinv b in FP64 (one CTA)
+template <class T>
+__global__ void __launch_bounds__(1024) k_coarse_solve(int n, T* b, T* x, const double* __restrict__ Cinv, int mean_project) {
+    extern __shared__ double sb[];
+    __shared__ double red[32];
+    double s = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double v = (double)b[i];
+        sb[i] = v;
+        s += v;
+    }
+    if (mean_project) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+            red[0] = t / n;
+        }
+        __syncthreads();
+        const double mean = red[0];
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            sb[i] -= mean;
+            b[i] = (T)sb[i];
+        }
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int row = w; row < n; row += nw) {
+        double a = 0;
+        for (int c = lane; c < n; c += 32) a += Cinv[(size_t)row * n + c] * sb[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) x[row] = (T)a;
+    }
+}
+
+template <class T>
+__global__ void k_mean_project(int n, T* b) {
+    __shared__ double red[32];
+    double s = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += (double)b[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        red[0] = t / n;
+    }
+    __syncthreads();
+    const double mean = red[0];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) b[i] = (T)((double)b[i] - mean);
+}
+
+// ----------------------------------------------------------------- V-cycle --
+template <class T>
+static void relax(mgldg_mg* m, int i, int n, bool reverse) {
+    LevelData& L = m->L[i];
+    const T* vals = bsr_vals<T>(L.A);
+    for (int k = 0; k < n; ++k) {
+        if (m->p.relaxation == MGLDG_RELAX_JACOBI) {
+            jacobi_sweep<T>(m->ctx, L.A, vals, LV<T>::D(L), LV<T>::b(L), LV<T>::x(L), LV<T>::xt(L), (T)m->p.omega);
+            std::swap(LV<T>::x(L), LV<T>::xt(L));
+        } else {
+            gs_sweep<T>(m->ctx, L.A, vals, LV<T>::D(L), LV<T>::b(L), LV<T>::x(L), L.sched, (T)m->p.omega, reverse);
+        }
+    }
+}
+
+template <class T>
+static void coarse_solve(mgldg_mg* m, int i) {
+    LevelData& L = m->L[i];
+    mgldg_ctx* ctx = m->ctx;
+    if (m->p.solver == MGLDG_COARSE_RELAXATION) {
+        if (m->p.mean_project) {
+            Launch K(ctx, MGLDG_K_COARSE);
+            k_mean_project<T><<<1, 1024, 0, ctx->stream>>>((int)L.n, LV<T>::b(L));
+        }
+        check_launch();
+        relax<T>(m, i, m->p.npre, false);
+        relax<T>(m, i, m->p.npost, true);
+        return;
+    }
+    {
+        Launch K(ctx, MGLDG_K_COARSE);
+        k_coarse_solve<T><<<1, 1024, L.n * sizeof(double), ctx->stream>>>((int)L.n, LV<T>::b(L), LV<T>::x(L), m->Cinv,
+                                                                          m->p.mean_project);
+    }
+    check_launch();
+}
+
+template <class T>
+static void vcycle(mgldg_mg* m, int i) {
+    mgldg_ctx* ctx = m->ctx;
+    if (i == (int)m->L.size() - 1) {
+        coarse_solve<T>(m, i);
+        return;
+    }
+    LevelData& L = m->L[i];
+    LevelData& C = m->L[i + 1];
+    relax<T>(m, i, m->p.npre, false);
+    // r = b - A x ; b_c = T^T r ; x_c = 0
+    spmv<T>(ctx, L.A, T(-1), LV<T>::x(L), T(1), LV<T>::b(L), LV<T>::r(L));
+    spmv<T>(ctx, L.Tt, T(1), LV<T>::r(L), T(0), (const T*)nullptr, LV<T>::b(C), nullptr, nullptr, nullptr,
+            MGLDG_K_TRANSFER);
+    MG_CHECK_CUDA(cudaMemsetAsync(LV<T>::x(C), 0, C.n * sizeof(T), ctx->stream));
+    vcycle<T>(m, i + 1);
+    // x += T x_c
+    spmv<T>(ctx, L.T, T(1), LV<T>::x(C), T(1), LV<T>::x(L), LV<T>::x(L), nullptr, nullptr, nullptr, MGLDG_K_TRANSFER);
+    relax<T>(m, i, m->p.npost, true);
+}
+
+static void take_errors(mgldg_mg* m) {
+    int e = 0;
+    for (auto& L : m->L)
+        if (L.has_sched) e |= gs_take_error(m->ctx, L.sched);
+    if (e) throw Error(MGLDG_ERR_TIMEOUT, "a Gauss-Seidel dependency wait ran out");
+}
+
+// one V-cycle on device vectors b (FP64) and x (FP64, in/out)
+static void vcycle_dev(mgldg_mg* m, const double* b, double* x, bool x_is_zero) {
+    mgldg_ctx* ctx = m->ctx;
+    LevelData& L = m->L[0];
+    if (m->p.precision == MGLDG_PREC_MIXED) {
+        convert<double, float>(ctx, L.n, b, L.b32);
+        if (x_is_zero) MG_CHECK_CUDA(cudaMemsetAsync(L.x32, 0, L.n * sizeof(float), ctx->stream));
+        else convert<double, float>(ctx, L.n, x, L.x32);
+        vcycle<float>(m, 0);
+        convert<float, double>(ctx, L.n, L.x32, x);
+    } else {
+        MG_CHECK_CUDA(cudaMemcpyAsync(L.bb, b, L.n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+        if (x_is_zero) MG_CHECK_CUDA(cudaMemsetAsync(L.x, 0, L.n * sizeof(double), ctx->stream));
+        else MG_CHECK_CUDA(cudaMemcpyAsync(L.x, x, L.n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+        vcycle<double>(m, 0);
+        MG_CHECK_CUDA(cudaMemcpyAsync(x, L.x, L.n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+}
+
+// -------------------------------------------------------------------- PCG --
+__global__ void k_pcg_init(PcgScalars* sc, const double* partials, int np) {
+    // delta_new = delta_0 = r.d
+    __shared__ double sm[32];
+    double s = 0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) s += partials[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sm[w];
+        sc->delta_new = t;
+        sc->delta0 = t;
+        sc->breakdown = 0;
+    }
+}
+
+__device__ double block_total(const double* partials, int np, double* sm) {
+    double s = 0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) s += partials[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    double t = 0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sm[w];
+    __syncthreads();
+    return t;
+}
+
+__global__ void k_pcg_alpha(PcgScalars* sc, const double* partials, int np) {
+    __shared__ double sm[32];
+    double dq = block_total(partials, np, sm);
+    if (threadIdx.x == 0) {
+        sc->dq = dq;
+        double a = sc->delta_new / dq;
+        if (!(dq > 0.0) || !isfinite(a)) sc->breakdown = 1;
+        sc->alpha = a;
+    }
+}
+
+__global__ void k_pcg_rr(PcgScalars* sc, const double* partials, int np, double* hist, int it) {
+    __shared__ double sm[32];
+    double rr = block_total(partials, np, sm);
+    if (threadIdx.x == 0) {
+        sc->rr = rr;
+        hist[it] = sqrt(rr);
+    }
+}
+
+__global__ void k_pcg_beta(PcgScalars* sc, const double* partials, int np) {
+    __shared__ double sm[32];
+    double rs = block_total(partials, np, sm);
+    if (threadIdx.x == 0) {
+        sc->delta_old = sc->delta_new;
+        sc->delta_new = rs;
+        double b = rs / sc->delta_old;
+        if (!isfinite(b)) sc->breakdown = 1;
+        sc->beta = b;
+    }
+}
+
+// x += alpha d ; (r -= alpha q) ; partial r.r
+__global__ void __launch_bounds__(256) k_pcg_update(int64_t n, const PcgScalars* sc, const double* __restrict__ d,
+                                                    const double* __restrict__ q, double* __restrict__ x,
+                                                    double* __restrict__ r, int update_r, double* partials) {
+    __shared__ double sm[8];
+    const double alpha = sc->alpha;
+    double s = 0;
+    for (int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (int64_t)gridDim.x * 256) {
+        x[i] += alpha * d[i];
+        if (update_r) {
+            double v = r[i] - alpha * q[i];
+            r[i] = v;
+            s += v * v;
+        }
+    }
+    if (update_r) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0;
+            for (int w = 0; w < 8; ++w) t += sm[w];
+            partials[blockIdx.x] = t;
+        }
+    }
+}
+
+// d = s + beta d
+__global__ void __launch_bounds__(256) k_pcg_dir(int64_t n, const PcgScalars* sc, const double* __restrict__ s,
+                                                 double* __restrict__ d) {
+    const double beta = sc->beta;
+    for (int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (int64_t)gridDim.x * 256)
+        d[i] = s[i] + beta * d[i];
+}
+
+static void ensure_pcg(mgldg_mg* m, mgldg_ctx* ctx, int64_t n, int maxit) {
+    if (m->pcg_n != n) {
+        dfree(m->r); dfree(m->d); dfree(m->q); dfree(m->s);
+        m->r = dalloc<double>(n); m->d = dalloc<double>(n); m->q = dalloc<double>(n); m->s = dalloc<double>(n);
+        m->pcg_n = n;
+    }
+    if (m->pcg_maxit < maxit) {
+        dfree(m->hist);
+        m->hist = dalloc<double>(std::max(1, maxit));
+        m->pcg_maxit = maxit;
+    }
+    if (!m->sc) {
+        m->sc = dalloc<PcgScalars>(1);
+        MG_CHECK_CUDA(cudaMallocHost(&m->h_sc, sizeof(PcgScalars)));
+    }
+}
+
+static void precon(mgldg_mg* m, const double* r, double* s) {
+    if (m->L.empty()) {
+        MG_CHECK_CUDA(cudaMemcpyAsync(s, r, m->pcg_n * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream));
+    } else {
+        vcycle_dev(m, r, s, true);
+    }
+}
+
+// pcg on device vectors (krylov.h:22-68)
+static void pcg_dev(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const double* b, double* x, double tol,
+                    int maxit, int* iters, double* res_hist) {
+    const int64_t n = (int64_t)A->nbr * A->br;
+    const int grid_vec = reduce_grid((int)std::min<int64_t>(n, 1 << 30));
+    ensure_pcg(m, ctx, n, std::max(1, maxit));
+    double* part = ctx->d_partials;
+    int np = 0;
+    // r = b - A x ; d = M(r) ; delta_new = delta_0 = r.d
+    spmv<double>(ctx, A, -1.0, x, 1.0, b, m->r);
+    precon(m, m->r, m->d);
+    dot_partials<double>(ctx, (int)n, m->r, m->d, part, &np);
+    {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_pcg_init<<<1, 256, 0, ctx->stream>>>(m->sc, part, np);
+    }
+    check_launch();
+    MG_CHECK_CUDA(cudaMemcpyAsync(m->h_sc, m->sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost, ctx->stream));
+    sync(ctx);
+    take_errors(m);
+    const double tol2 = tol * tol;
+    int i = 0;
+    bool broke = false;
+    while (i < maxit && m->h_sc->delta_new > tol2 * m->h_sc->delta0) {
+        // q = A d ; alpha = delta_new / d.q
+        spmv<double>(ctx, A, 1.0, m->d, 0.0, nullptr, m->q, m->d, part, &np);
+        {
+            Launch L(ctx, MGLDG_K_VECTOR);
+            k_pcg_alpha<<<1, 256, 0, ctx->stream>>>(m->sc, part, np);
+        }
+        check_launch();
+        if (i % 50 == 0) {
+            // x += alpha d ; r = b - A x (residual replacement)
+            {
+                Launch L(ctx, MGLDG_K_VECTOR);
+                k_pcg_update<<<grid_vec, 256, 0, ctx->stream>>>(n, m->sc, m->d, m->q, x, m->r, 0, part);
+            }
+            check_launch();
+            spmv<double>(ctx, A, -1.0, x, 1.0, b, m->r, m->r, part, &np);
+        } else {
+            {
+                Launch L(ctx, MGLDG_K_VECTOR);
+                k_pcg_update<<<grid_vec, 256, 0, ctx->stream>>>(n, m->sc, m->d, m->q, x, m->r, 1, part);
+            }
+            check_launch();
+            np = grid_vec;
+        }
+        {
+            Launch L(ctx, MGLDG_K_VECTOR);
+            k_pcg_rr<<<1, 256, 0, ctx->stream>>>(m->sc, part, np, m->hist, i);
+        }
+        check_launch();
+        // s = M(r) ; delta_new = r.s ; beta ; d = s + beta d
+        precon(m, m->r, m->s);
+        dot_partials<double>(ctx, (int)n, m->r, m->s, part, &np);
+        {
+            Launch L(ctx, MGLDG_K_VECTOR);
+            k_pcg_beta<<<1, 256, 0, ctx->stream>>>(m->sc, part, np);
+        }
+        check_launch();
+        {
+            Launch L(ctx, MGLDG_K_VECTOR);
+            k_pcg_dir<<<grid_vec, 256, 0, ctx->stream>>>(n, m->sc, m->s, m->d);
+        }
+        check_launch();
+        MG_CHECK_CUDA(cudaMemcpyAsync(m->h_sc, m->sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost, ctx->stream));
+        sync(ctx);
+        ++i;
+        if (m->h_sc->breakdown) { broke = true; break; }
+    }
+    take_errors(m);
+    if (iters) *iters = i;
+    if (res_hist && i > 0) {
+        download(ctx, res_hist, m->hist, i);
+        sync(ctx);
+    }
+    if (broke) throw Error(MGLDG_ERR_BREAKDOWN, "pcg breakdown (d.q <= 0 or a non-finite scalar)");
+}
+
+}  // namespace mg
+
+mgldg_mg::~mgldg_mg() {
+    if (ctx) cudaSetDevice(ctx->device);
+    for (auto& L : this->L) {
+        if (L.owns_ops) delete L.ops;
+        dfree(L.Dinv); dfree(L.Dinv32);
+        if (L.has_sched) sched_free(L.sched);
+        dfree(L.x); dfree(L.bb); dfree(L.r); dfree(L.xt);
+        dfree(L.x32); dfree(L.b32); dfree(L.r32); dfree(L.xt32);
+        delete L.T;
+        delete L.Tt;
+    }
+    dfree(Cinv);
+    dfree(r); dfree(d); dfree(q); dfree(s); dfree(hist);
+    dfree(sc);
+    if (h_sc) cudaFreeHost(h_sc);
+}
+
+// ================================================================== C ABI ==
+extern "C" void mgldg_mg_params_default(mgldg_mg_params* p) {
+    if (!p) return;
+    p->relaxation = MGLDG_RELAX_GAUSS_SEIDEL;
+    p->omega = 0.8;
+    p->solver = MGLDG_COARSE_CHOLESKY;
+    p->npre = 3;
+    p->npost = 3;
+    p->restriction = MGLDG_RESTRICT_RATRAT;
+    p->precision = MGLDG_PREC_FP64;
+    p->max_levels = 0;
+    p->mean_project = 1;
+}
+
+static void level_alloc(mgldg_ctx* ctx, mgldg_mg* m, LevelData& L, bool need_sched) {
+    L.A = L.ops->A;
+    L.ne = L.A->nbr;
+    L.b = L.A->br;
+    L.n = (int64_t)L.ne * L.b;
+    bsr_build_diag(const_cast<mgldg_bsr*>(L.A));
+    for (int i = 0; i < L.ne; ++i)
+        MG_REQUIRE(L.A->h_diag[i] >= 0, MGLDG_ERR_SHAPE, "level matrix lacks a diagonal block");
+    // inverse diagonal blocks (the reference's Dinv LDL^T factors)
+    int* dstatus = dalloc<int>(1);
+    try {
+        MG_CHECK_CUDA(cudaMemsetAsync(dstatus, 0, sizeof(int), ctx->stream));
+        L.Dinv = dalloc<double>((size_t)L.ne * L.b * L.b);
+        block_inverse(ctx, L.A, L.Dinv, dstatus);
+        int h = 0;
+        download(ctx, &h, dstatus, 1);
+        sync(ctx);
+        MG_REQUIRE(h == 0, MGLDG_ERR_NOT_SPD, "singular diagonal block in a level matrix");
+    } catch (...) {
+        dfree(dstatus);
+        throw;
+    }
+    dfree(dstatus);
+    const bool mixed = m->p.precision == MGLDG_PREC_MIXED;
+    if (mixed) {
+        bsr_ensure_fp32(const_cast<mgldg_bsr*>(L.A));
+        L.Dinv32 = dalloc<float>((size_t)L.ne * L.b * L.b);
+        convert<double, float>(ctx, (int64_t)L.ne * L.b * L.b, L.Dinv, L.Dinv32);
+        L.x32 = dalloc<float>(L.n); L.b32 = dalloc<float>(L.n); L.r32 = dalloc<float>(L.n); L.xt32 = dalloc<float>(L.n);
+    } else {
+        L.x = dalloc<double>(L.n); L.bb = dalloc<double>(L.n); L.r = dalloc<double>(L.n); L.xt = dalloc<double>(L.n);
+    }
+    if (need_sched) {
+        sched_build(ctx, L.A, L.sched);
+        L.has_sched = true;
+    }
+}
+
+extern "C" int mgldg_mg_create(mgldg_ctx* ctx, const mgldg_ops* fine, const mgldg_bsr* const* T, int nT,
+                               const mgldg_mg_params* params, mgldg_mg** out) {
+    MG_API_BEGIN(ctx)
+    MG_REQUIRE(out && fine && params && nT >= 0 && (nT == 0 || T), MGLDG_ERR_ARG, "bad multigrid arguments");
+    *out = nullptr;
+    const mgldg_mg_params& p = *params;
+    MG_REQUIRE(p.relaxation == MGLDG_RELAX_JACOBI || p.relaxation == MGLDG_RELAX_GAUSS_SEIDEL, MGLDG_ERR_ARG,
+               "Unknown relaxation method.");
+    MG_REQUIRE(p.solver == MGLDG_COARSE_CHOLESKY || p.solver == MGLDG_COARSE_RELAXATION ||
+                   p.solver == MGLDG_COARSE_DENSE, MGLDG_ERR_ARG, "Unknown coarse solver.");
+    MG_REQUIRE(p.restriction == MGLDG_RESTRICT_RAT || p.restriction == MGLDG_RESTRICT_RATRAT, MGLDG_ERR_ARG,
+               "Unknown restriction method.");
+    MG_REQUIRE(p.precision == MGLDG_PREC_FP64 || p.precision == MGLDG_PREC_MIXED, MGLDG_ERR_ARG, "Unknown precision.");
+    MG_REQUIRE(p.npre >= 0 && p.npost >= 0, MGLDG_ERR_ARG, "negative smoothing count");
+    MG_REQUIRE(fine->A != nullptr, MGLDG_ERR_ARG, "fine operators lack A (call construct_laplacian)");
+    mgldg_mg* m = new mgldg_mg();
+    m->ctx = ctx;
+    m->p = p;
+    try {
+        const int use = (p.max_levels <= 0) ? nT : std::min(nT, p.max_levels - 1);
+        m->L.resize(use + 1);
+        m->L[0].ops = const_cast<mgldg_ops*>(fine);
+        m->L[0].owns_ops = false;
+        for (int i = 0; i < use; ++i) {
+            const mgldg_bsr* Ti = T[i];
+            MG_REQUIRE(Ti != nullptr, MGLDG_ERR_ARG, "null interpolation operator");
+            const mgldg_ops* f = m->L[i].ops;
+            MG_REQUIRE(Ti->nbr == f->A->nbr && Ti->br == f->A->br, MGLDG_ERR_SHAPE,
+                       "interpolation rows do not match the finer level");
+            // transfers: private copy with repeated blocks collapsed, and its transpose
+            mgldg_bsr* Tc = bsr_clone(ctx, Ti);
+            m->L[i].T = Tc;
+            bsr_dedupe(ctx, Tc);
+            m->L[i].Tt = bsr_transpose(ctx, Tc);
+            mgldg_ops* c = (p.restriction == MGLDG_RESTRICT_RATRAT) ? galerkin_ratrat(ctx, f, Tc) : galerkin_rat(ctx, f, Tc);
+            m->L[i + 1].ops = c;
+            m->L[i + 1].owns_ops = true;
+            if (p.precision == MGLDG_PREC_MIXED) {
+                bsr_ensure_fp32(Tc);
+                bsr_ensure_fp32(m->L[i].Tt);
+            }
+        }
+        const int last = use;
+        for (int i = 0; i <= last; ++i) {
+            bool sched = p.relaxation == MGLDG_RELAX_GAUSS_SEIDEL && (i < last || p.solver == MGLDG_COARSE_RELAXATION);
+            level_alloc(ctx, m, m->L[i], sched);
+        }
+        if (p.solver != MGLDG_COARSE_RELAXATION) {
+            const mgldg_bsr* Ac = m->L[last].A;
+            if (p.solver == MGLDG_COARSE_CHOLESKY)
+                MG_REQUIRE(Ac->nbr == 1, MGLDG_ERR_ARG,
+                           "Cholesky coarse solve needs a one-element coarsest level (use MGLDG_COARSE_DENSE)");
+            m->nc = Ac->nbr * Ac->br;
+            MG_REQUIRE(m->nc <= 4096, MGLDG_ERR_UNSUPPORTED, "dense coarsest solve limited to 4096 unknowns");
+            m->Cinv = dalloc<double>((size_t)m->nc * m->nc);
+            dense_spd_inverse(ctx, Ac, m->Cinv);
+        }
+        sync(ctx);
+    } catch (...) {
+        delete m;
+        throw;
+    }
+    *out = m;
+    MG_API_END
+}
+
+extern "C" int mgldg_mg_destroy(mgldg_mg* m) {
+    delete m;
+    return MGLDG_OK;
+}
+
+extern "C" int mgldg_mg_nlevels(const mgldg_mg* m, int* n) {
+    if (!m || !n) return MGLDG_ERR_ARG;
+    *n = (int)m->L.size();
+    return MGLDG_OK;
+}
+
+extern "C" int mgldg_mg_level_op(const mgldg_mg* m, int level, int which, const mgldg_bsr** A) {
+    if (!m || level < 0 || level >= (int)m->L.size()) return MGLDG_ERR_ARG;
+    return mgldg_ops_get(m->L[level].ops, which, A);
+}
+
+extern "C" int mgldg_mg_vcycle_dev(mgldg_ctx* ctx, mgldg_mg* m, const double* b, double* x) {
+    MG_API_BEGIN(ctx)
+    MG_REQUIRE(m && b && x, MGLDG_ERR_ARG, "null argument");
+    vcycle_dev(m, b, x, false);
+    MG_API_END
+}
+
+extern "C" int mgldg_mg_vcycle(mgldg_ctx* ctx, mgldg_mg* m, const double* b, double* x) {
+    MG_API_BEGIN(ctx)
+    MG_REQUIRE(m && b && x, MGLDG_ERR_ARG, "null argument");
+    const int64_t n = m->L[0].n;
+    double *db = nullptr, *dx = nullptr;
+    try {
+        db = dalloc<double>(n);
+        dx = dalloc<double>(n);
+        upload(ctx, db, b, n);
+        upload(ctx, dx, x, n);
+        vcycle_dev(m, db, dx, false);
+        download(ctx, x, dx, n);
+        sync(ctx);
+        take_errors(m);
+    } catch (...) {
+        dfree(db);
+        dfree(dx);
+        throw;
+    }
+    dfree(db);
+    dfree(dx);
+    MG_API_END
+}
+
+extern "C" int mgldg_mg_relax(mgldg_ctx* ctx, mgldg_mg* m, int level, int n, int reverse, const double* b, double* x) {
+    MG_API_BEGIN(ctx)
+    MG_REQUIRE(m && b && x && level >= 0 && level < (int)m->L.size() && n >= 0, MGLDG_ERR_ARG, "bad relax arguments");
+    LevelData& L = m->L[level];
+    MG_REQUIRE(m->p.relaxation == MGLDG_RELAX_JACOBI || L.has_sched, MGLDG_ERR_ARG, "no smoother schedule on this level");
+    double *db = nullptr, *dx = nullptr;
+    try {
+        db = dalloc<double>(L.n);
+        dx = dalloc<double>(L.n);
+        upload(ctx, db, b, L.n);
+        upload(ctx, dx, x, L.n);
+        if (m->p.precision == MGLDG_PREC_MIXED) {
+            convert<double, float>(ctx, L.n, db, L.b32);
+            convert<double, float>(ctx, L.n, dx, L.x32);
+            relax<float>(m, level, n, reverse != 0);
+            convert<float, double>(ctx, L.n, L.x32, dx);
+        } else {
+            MG_CHECK_CUDA(cudaMemcpyAsync(L.bb, db, L.n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+            MG_CHECK_CUDA(cudaMemcpyAsync(L.x, dx, L.n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+            relax<double>(m, level, n, reverse != 0);
+            MG_CHECK_CUDA(cudaMemcpyAsync(dx, L.x, L.n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+        }
+        download(ctx, x, dx, L.n);
+        sync(ctx);
+        take_errors(m);
+    } catch (...) {
+        dfree(db);
+        dfree(dx);
+        throw;
+    }
+    dfree(db);
+    dfree(dx);
+    MG_API_END
+}
+
+extern "C" int mgldg_pcg_dev(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const double* b, double* x, double tol,
+                             int maxit, int* iters, double* res_hist) {
+    MG_API_BEGIN(ctx)
+    MG_REQUIRE(A && b && x && maxit >= 0, MGLDG_ERR_ARG, "bad pcg arguments");
+    MG_REQUIRE(A->br == A->bc && A->nbr == A->nbc, MGLDG_ERR_SHAPE, "pcg needs a square matrix");
+    if (m) MG_REQUIRE(m->L[0].n == (int64_t)A->nbr * A->br, MGLDG_ERR_SHAPE, "preconditioner size mismatch");
+    if (m) {
+        pcg_dev(ctx, m, A, b, x, tol, maxit, iters, res_hist);
+    } else {
+        // unpreconditioned overload (krylov.h:78-82): a level-free holder
+        // owns the work space for this call only
+        mgldg_mg plain;
+        plain.ctx = ctx;
+        mgldg_mg_params_default(&plain.p);
+        pcg_dev(ctx, &plain, A, b, x, tol, maxit, iters, res_hist);
+    }
+    MG_API_END
+}
+
+extern "C" int mgldg_pcg(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const double* b, double* x, double tol,
+                         int maxit, int* iters, double* res_hist) {
+    MG_API_BEGIN(ctx)
+    MG_REQUIRE(A && b && x && maxit >= 0, MGLDG_ERR_ARG, "bad pcg arguments");
+    MG_REQUIRE(A->br == A->bc && A->nbr == A->nbc, MGLDG_ERR_SHAPE, "pcg needs a square matrix");
+    if (m) MG_REQUIRE(m->L[0].n == (int64_t)A->nbr * A->br, MGLDG_ERR_SHAPE, "preconditioner size mismatch");
+    const int64_t n = (int64_t)A->nbr * A->br;
+    double *db = nullptr, *dx = nullptr;
+    try {
+        db = dalloc<double>(n);
+        dx = dalloc<double>(n);
+        upload(ctx, db, b, n);
+        upload(ctx, dx, x, n);
+        if (m) {
+            pcg_dev(ctx, m, A, db, dx, tol, maxit, iters, res_hist);
+        } else {
+            mgldg_mg plain;
+            plain.ctx = ctx;
+            mgldg_mg_params_default(&plain.p);
+            pcg_dev(ctx, &plain, A, db, dx, tol, maxit, iters, res_hist);
+        }
+        download(ctx, x, dx, n);
+        sync(ctx);
+    } catch (...) {
+        dfree(db);
+        dfree(dx);
+        throw;
+    }
+    dfree(db);
+    dfree(dx);
+    MG_API_END
+}

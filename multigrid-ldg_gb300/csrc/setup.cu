@@ -1,0 +1,715 @@
+// setup.cu -- Galerkin coarsening setup: block SpGEMM (symbolic on the host,
+// numeric on the GPU), batched block inverses, the Laplacian triple product
+// and the dense inverse of the coarsest level.
+//
+// Follows the reference's Level coarse constructor
+// (src/cartesian/multigrid/multigrid.h:105-171), construct_laplacian
+// (src/cartesian/dg/ldgpoisson.h:34-52) and multiply_mm / multiply_mm_t
+// (src/cartesian/util/sparseblockmatrix.tpp:234-280).
+//
+// A product plan lists, for every output block, the ordered terms that sum
+// into it.  The numeric kernel gives each output block to one CTA (one thread
+// per block entry); each term's operands are staged in shared memory, so the
+// sum over terms runs in a fixed order (the reference's order over d and k),
+// and every output block is computed by exactly one CTA.
+#include <algorithm>
+#include <numeric>
+
+#include "api.cuh"
+
+using namespace mg;
+
+namespace mg {
+
+struct Term {
+    int x, m, y;
+};
+
+// output pattern + ordered terms per output block
+struct Plan {
+    int nbr = 0, nbc = 0;
+    std::vector<int> row_ptr, col_idx;
+    std::vector<int> tptr;
+    std::vector<Term> terms;
+};
+
+struct KeyTerm {
+    int64_t key;
+    Term t;
+};
+
+static void finish_plan(Plan& P, std::vector<KeyTerm>& kt, const std::vector<int64_t>* force_keys) {
+    // stable: keeps the generation order of terms inside one output block
+    std::stable_sort(kt.begin(), kt.end(), [](const KeyTerm& a, const KeyTerm& b) { return a.key < b.key; });
+    std::vector<int64_t> keys;
+    keys.reserve(kt.size() + (force_keys ? force_keys->size() : 0));
+    for (auto& e : kt) keys.push_back(e.key);
+    if (force_keys) keys.insert(keys.end(), force_keys->begin(), force_keys->end());
+    std::sort(keys.begin(), keys.end());
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    P.row_ptr.assign(P.nbr + 1, 0);
+    P.col_idx.resize(keys.size());
+    for (size_t q = 0; q < keys.size(); ++q) {
+        int i = (int)(keys[q] / P.nbc);
+        P.col_idx[q] = (int)(keys[q] - (int64_t)i * P.nbc);
+        P.row_ptr[i + 1]++;
+    }
+    for (int i = 0; i < P.nbr; ++i) P.row_ptr[i + 1] += P.row_ptr[i];
+    P.tptr.assign(keys.size() + 1, 0);
+    P.terms.resize(kt.size());
+    size_t q = 0;
+    for (size_t e = 0; e < kt.size(); ++e) {
+        while (keys[q] != kt[e].key) ++q;
+        P.tptr[q + 1]++;
+        P.terms[e] = kt[e].t;
+    }
+    for (size_t o = 0; o < keys.size(); ++o) P.tptr[o + 1] += P.tptr[o];
+}
+
+// C = op(X) * Y   (multiply_mm when !tX, multiply_mm_t when tX)
+static Plan plan_mm(const mgldg_bsr* X, bool tX, const mgldg_bsr* Y) {
+    Plan P;
+    std::vector<KeyTerm> kt;
+    if (!tX) {
+        MG_REQUIRE(X->nbc == Y->nbr && X->bc == Y->br, MGLDG_ERR_SHAPE, "multiply_mm: shapes do not conform");
+        P.nbr = X->nbr; P.nbc = Y->nbc;
+        for (int i = 0; i < X->nbr; ++i)
+            for (int a = X->h_row_ptr[i]; a < X->h_row_ptr[i + 1]; ++a) {
+                int k = X->h_col_idx[a];
+                for (int b = Y->h_row_ptr[k]; b < Y->h_row_ptr[k + 1]; ++b)
+                    kt.push_back({(int64_t)i * P.nbc + Y->h_col_idx[b], Term{a, -1, b}});
+            }
+    } else {
+        MG_REQUIRE(X->nbr == Y->nbr && X->br == Y->br, MGLDG_ERR_SHAPE, "multiply_mm_t: shapes do not conform");
+        P.nbr = X->nbc; P.nbc = Y->nbc;
+        // column view of X: rows k of column i in ascending order
+        std::vector<int> cp(X->nbc + 1, 0);
+        for (int64_t a = 0; a < X->nnzb; ++a) cp[X->h_col_idx[a] + 1]++;
+        for (int j = 0; j < X->nbc; ++j) cp[j + 1] += cp[j];
+        std::vector<int> pos(cp.begin(), cp.end() - 1), ck(X->nnzb), ca(X->nnzb);
+        for (int k = 0; k < X->nbr; ++k)
+            for (int a = X->h_row_ptr[k]; a < X->h_row_ptr[k + 1]; ++a) {
+                int p = pos[X->h_col_idx[a]]++;
+                ck[p] = k;
+                ca[p] = a;
+            }
+        for (int i = 0; i < X->nbc; ++i)
+            for (int p = cp[i]; p < cp[i + 1]; ++p) {
+                int k = ck[p], a = ca[p];
+                for (int b = Y->h_row_ptr[k]; b < Y->h_row_ptr[k + 1]; ++b)
+                    kt.push_back({(int64_t)i * P.nbc + Y->h_col_idx[b], Term{a, -1, b}});
+            }
+    }
+    finish_plan(P, kt, nullptr);
+    return P;
+}
+
+// sum over rows k of  X(k,i)^T D(k,k) X(k,j)  for i, j in cols(X, k):
+// the triple product of construct_laplacian (one dimension) and of the
+// coarse mass matrix.  `extra` adds output keys (the T pattern).
+static Plan plan_triple(const std::vector<const mgldg_bsr*>& Xs, const mgldg_bsr* D, const mgldg_bsr* extra,
+                        std::vector<Plan>* per_dim) {
+    const mgldg_bsr* X0 = Xs[0];
+    int nout = X0->nbc;
+    std::vector<int64_t> allkeys;
+    std::vector<std::vector<KeyTerm>> kts(Xs.size());
+    for (size_t d = 0; d < Xs.size(); ++d) {
+        const mgldg_bsr* X = Xs[d];
+        MG_REQUIRE(X->nbr == D->nbr && X->br == D->bc, MGLDG_ERR_SHAPE, "triple product: shapes do not conform");
+        for (int k = 0; k < X->nbr; ++k) {
+            int m = D->h_diag[k];
+            MG_REQUIRE(m >= 0, MGLDG_ERR_SHAPE, "mass matrix lacks a diagonal block");
+            for (int a = X->h_row_ptr[k]; a < X->h_row_ptr[k + 1]; ++a)
+                for (int b = X->h_row_ptr[k]; b < X->h_row_ptr[k + 1]; ++b) {
+                    int64_t key = (int64_t)X->h_col_idx[a] * nout + X->h_col_idx[b];
+                    kts[d].push_back({key, Term{a, m, b}});
+                    allkeys.push_back(key);
+                }
+        }
+    }
+    if (extra)
+        for (int i = 0; i < extra->nbr; ++i)
+            for (int a = extra->h_row_ptr[i]; a < extra->h_row_ptr[i + 1]; ++a)
+                allkeys.push_back((int64_t)i * nout + extra->h_col_idx[a]);
+    std::sort(allkeys.begin(), allkeys.end());
+    allkeys.erase(std::unique(allkeys.begin(), allkeys.end()), allkeys.end());
+    Plan U;
+    U.nbr = nout; U.nbc = nout;
+    std::vector<KeyTerm> none;
+    finish_plan(U, none, &allkeys);
+    per_dim->clear();
+    for (size_t d = 0; d < Xs.size(); ++d) {
+        Plan P;
+        P.nbr = nout; P.nbc = nout;
+        finish_plan(P, kts[d], &allkeys);
+        per_dim->push_back(std::move(P));
+    }
+    return U;
+}
+
+// ------------------------------------------------------------ numeric ------
+struct Opnd {
+    const double* val;
+    const int* blk;
+    int r, c;
+    __device__ __forceinline__ const double* at(int k) const {
+        return val + (size_t)(blk ? blk[k] : k) * r * c;
+    }
+};
+
+// out[o] = init[o] (or 0) + sum_t opX(X[t.x]) * (M[t.m]) * Y[t.y]
+__global__ void __launch_bounds__(1024)
+    k_prod(int nout, int oR, int oC, Opnd X, int tX, Opnd Mm, Opnd Y, const int* __restrict__ tptr,
+           const int3* __restrict__ terms, const double* init, double* out) {
+    extern __shared__ double sm[];
+    double* sX = sm;
+    double* sM = sX + 1024;
+    double* sY = sM + 1024;
+    double* sW = sY + 1024;
+    const int inner = tX ? X.r : X.c;   // columns of op(X)
+    const int nth = blockDim.x;
+    const int nent = oR * oC;
+    for (int o = blockIdx.x; o < nout; o += gridDim.x) {
+        double acc[1];
+        const int e = threadIdx.x;
+        const int r = e / oC, s = e - r * oC;
+        acc[0] = (init && e < nent) ? init[(size_t)o * nent + e] : 0.0;
+        for (int t = tptr[o]; t < tptr[o + 1]; ++t) {
+            const int3 tm = terms[t];
+            const double* px = X.at(tm.x);
+            const double* py = Y.at(tm.z);
+            for (int q = threadIdx.x; q < X.r * X.c; q += nth) sX[q] = px[q];
+            for (int q = threadIdx.x; q < Y.r * Y.c; q += nth) sY[q] = py[q];
+            if (tm.y >= 0) {
+                const double* pm = Mm.at(tm.y);
+                for (int q = threadIdx.x; q < Mm.r * Mm.c; q += nth) sM[q] = pm[q];
+            }
+            __syncthreads();
+            const double* Wp;
+            int wc;
+            if (tm.y >= 0) {
+                // W = op(X) * M   (oR x Mm.c)
+                for (int q = threadIdx.x; q < oR * Mm.c; q += nth) {
+                    int rr = q / Mm.c, cc = q - rr * Mm.c;
+                    double v = 0;
+                    for (int z = 0; z < inner; ++z) v += (tX ? sX[z * X.c + rr] : sX[rr * X.c + z]) * sM[z * Mm.c + cc];
+                    sW[q] = v;
+                }
+                __syncthreads();
+                Wp = sW;
+                wc = Mm.c;
+                if (e < nent) {
+                    double v = 0;
+                    for (int z = 0; z < wc; ++z) v += Wp[r * wc + z] * sY[z * Y.c + s];
+                    acc[0] += v;
+                }
+            } else if (e < nent) {
+                double v = 0;
+                for (int z = 0; z < inner; ++z) v += (tX ? sX[z * X.c + r] : sX[r * X.c + z]) * sY[z * Y.c + s];
+                acc[0] += v;
+            }
+            __syncthreads();
+        }
+        if (e < nent) out[(size_t)o * nent + e] = acc[0];
+        __syncthreads();
+    }
+}
+
+static Opnd opnd(const mgldg_bsr* A) { return Opnd{A->val, A->blk, A->br, A->bc}; }
+
+static void run_plan(mgldg_ctx* ctx, const Plan& P, int oR, int oC, Opnd X, bool tX, Opnd Mm, Opnd Y,
+                     const double* init, double* out) {
+    int nout = (int)P.col_idx.size();
+    if (nout == 0) return;
+    MG_REQUIRE(oR * oC <= 1024 && X.r * X.c <= 1024 && Y.r * Y.c <= 1024 && Mm.r * Mm.c <= 1024,
+               MGLDG_ERR_UNSUPPORTED, "block products limited to 32x32 blocks");
+    int* dptr = nullptr;
+    int3* dterms = nullptr;
+    try {
+        dptr = dalloc<int>(P.tptr.size());
+        dterms = dalloc<int3>(std::max<size_t>(1, P.terms.size()));
+        upload(ctx, dptr, P.tptr.data(), P.tptr.size());
+        upload(ctx, dterms, reinterpret_cast<const int3*>(P.terms.data()), P.terms.size());
+        int nth = ((oR * oC + 31) / 32) * 32;
+        int grid = std::min(nout, 1 << 20);
+        {
+            Launch L(ctx, MGLDG_K_SETUP);
+            k_prod<<<grid, nth, 4 * 1024 * sizeof(double), ctx->stream>>>(nout, oR, oC, X, tX ? 1 : 0, Mm, Y, dptr,
+                                                                          dterms, init, out);
+        }
+        check_launch();
+        sync(ctx);
+    } catch (...) {
+        dfree(dptr);
+        dfree(dterms);
+        throw;
+    }
+    dfree(dptr);
+    dfree(dterms);
+}
+
+static mgldg_bsr* new_from_plan(mgldg_ctx* ctx, const Plan& P, int br, int bc) {
+    return bsr_new(ctx, P.nbr, P.nbc, br, bc, P.row_ptr, P.col_idx);
+}
+
+// C = op(X) * Y as a new BSR
+static mgldg_bsr* mm(mgldg_ctx* ctx, const mgldg_bsr* X, bool tX, const mgldg_bsr* Y) {
+    Plan P = plan_mm(X, tX, Y);
+    int oR = tX ? X->bc : X->br, oC = Y->bc;
+    mgldg_bsr* C = new_from_plan(ctx, P, oR, oC);
+    try {
+        run_plan(ctx, P, oR, oC, opnd(X), tX, Opnd{nullptr, nullptr, 0, 0}, opnd(Y), nullptr, C->val);
+    } catch (...) {
+        delete C;
+        throw;
+    }
+    return C;
+}
+
+// ------------------------------------------------------- block inverses ----
+// Gauss-Jordan with partial pivoting, one warp per block (b <= 32).
+__global__ void k_block_inverse(int n, int b, const double* __restrict__ val, const int* __restrict__ blk,
+                                const int* __restrict__ pos, double* __restrict__ out, int* status) {
+    extern __shared__ double sm[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    const int w2 = 2 * b;
+    double* aug = sm + (size_t)warp * b * w2;
+    for (int i = blockIdx.x * wpb + warp; i < n; i += gridDim.x * wpb) {
+        const int p = pos ? pos[i] : i;
+        if (p < 0) {
+            if (lane == 0) atomicOr(status, 2);
+            continue;
+        }
+        const double* a = val + (size_t)(blk ? blk[p] : p) * b * b;
+        for (int q = lane; q < b * w2; q += 32) {
+            int r = q / w2, c = q - r * w2;
+            aug[q] = (c < b) ? a[r * b + c] : (c - b == r ? 1.0 : 0.0);
+        }
+        __syncwarp();
+        bool bad = false;
+        for (int k = 0; k < b; ++k) {
+            // pivot row: largest |aug(r,k)|, r >= k (first on ties)
+            double v = (lane >= k && lane < b) ? fabs(aug[lane * w2 + k]) : -1.0;
+            int idx = lane;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                double v2 = __shfl_xor_sync(0xffffffffu, v, o);
+                int i2 = __shfl_xor_sync(0xffffffffu, idx, o);
+                if (v2 > v || (v2 == v && i2 < idx)) { v = v2; idx = i2; }
+            }
+            if (!(v > 0.0) || !isfinite(v)) bad = true;
+            if (idx != k)
+                for (int c = lane; c < w2; c += 32) {
+                    double t = aug[k * w2 + c];
+                    aug[k * w2 + c] = aug[idx * w2 + c];
+                    aug[idx * w2 + c] = t;
+                }
+            __syncwarp();
+            const double inv = 1.0 / aug[k * w2 + k];
+            __syncwarp();
+            for (int c = lane; c < w2; c += 32) aug[k * w2 + c] *= inv;
+            __syncwarp();
+            // eliminate column k from the other rows; column k supplies the
+            // factors, so it is left untouched here and cleared afterwards
+            for (int c = lane; c < w2; c += 32) {
+                if (c == k) continue;
+                const double pk = aug[k * w2 + c];
+                for (int r = 0; r < b; ++r) {
+                    if (r == k) continue;
+                    aug[r * w2 + c] -= aug[r * w2 + k] * pk;
+                }
+            }
+            __syncwarp();
+            if (lane < b && lane != k) aug[lane * w2 + k] = 0.0;
+            __syncwarp();
+        }
+        if (bad && lane == 0) atomicOr(status, 1);
+        double* o = out + (size_t)i * b * b;
+        for (int q = lane; q < b * b; q += 32) {
+            int r = q / b, c = q - r * b;
+            o[q] = aug[r * w2 + b + c];
+        }
+        __syncwarp();
+    }
+}
+
+void block_inverse(mgldg_ctx* ctx, const mgldg_bsr* A, double* out, int* dstatus) {
+    MG_REQUIRE(A->br == A->bc && A->br <= 32, MGLDG_ERR_UNSUPPORTED, "block inverse needs square blocks <= 32");
+    MG_REQUIRE(A->diag != nullptr, MGLDG_ERR_ARG, "diagonal index not built");
+    const int b = A->br, wpb = 4;
+    size_t smem = (size_t)wpb * b * 2 * b * sizeof(double);
+    int grid = std::max(1, std::min((A->nbr + wpb - 1) / wpb, ctx->sm_count * 16));
+    {
+        Launch L(ctx, MGLDG_K_SETUP);
+        k_block_inverse<<<grid, wpb * 32, smem, ctx->stream>>>(A->nbr, b, A->val, A->blk, A->diag, out, dstatus);
+    }
+    check_launch();
+}
+
+static void check_status(mgldg_ctx* ctx, int* dstatus, const char* what) {
+    int h = 0;
+    download(ctx, &h, dstatus, 1);
+    sync(ctx);
+    if (h & 2) throw Error(MGLDG_ERR_SHAPE, std::string(what) + ": missing diagonal block");
+    if (h & 1) throw Error(MGLDG_ERR_NOT_SPD, std::string(what) + ": singular diagonal block");
+}
+
+// out[q] = A's block src[q] (zero block where src[q] < 0)
+__global__ void k_gather_blocks(int64_t n, int bsz, const int* __restrict__ src, const double* __restrict__ val,
+                                const int* __restrict__ blk, double* __restrict__ out) {
+    for (int64_t t = (int64_t)blockIdx.x * 256 + threadIdx.x; t < n * bsz; t += (int64_t)gridDim.x * 256) {
+        int64_t q = t / bsz;
+        int e = (int)(t - q * bsz);
+        int s = src[q];
+        out[t] = (s < 0) ? 0.0 : val[(size_t)(blk ? blk[s] : s) * bsz + e];
+    }
+}
+
+static void gather_blocks(mgldg_ctx* ctx, const std::vector<int>& src_of, const mgldg_bsr* A, double* out) {
+    int64_t n = (int64_t)src_of.size();
+    if (n == 0) return;
+    int* dsrc = dalloc<int>(n);
+    try {
+        upload(ctx, dsrc, src_of.data(), n);
+        int g = (int)std::min<int64_t>((n * (int64_t)A->bsz() + 255) / 256, ctx->sm_count * 32);
+        {
+            Launch L(ctx, MGLDG_K_SETUP);
+            k_gather_blocks<<<g, 256, 0, ctx->stream>>>(n, (int)A->bsz(), dsrc, A->val, A->blk, out);
+        }
+        check_launch();
+        sync(ctx);
+    } catch (...) {
+        dfree(dsrc);
+        throw;
+    }
+    dfree(dsrc);
+}
+
+// ------------------------------------------------------- construct_laplacian
+// A = T + sum_d sum_k G_d(k,:)^T M(k,k) G_d(k,:)   (ldgpoisson.h:34-52)
+static mgldg_bsr* laplacian(mgldg_ctx* ctx, mgldg_bsr* M, mgldg_bsr* const* G, int ndim, mgldg_bsr* T) {
+    bsr_build_diag(M);
+    std::vector<const mgldg_bsr*> Xs(G, G + ndim);
+    std::vector<Plan> per;
+    Plan U = plan_triple(Xs, M, T, &per);
+    const int b = T->br;
+    mgldg_bsr* A = new_from_plan(ctx, U, b, b);
+    double* initv = nullptr;
+    try {
+        // A starts as a copy of T scattered into the union pattern
+        initv = dalloc<double>(std::max<size_t>(1, U.col_idx.size() * A->bsz()));
+        std::vector<int> src_of(U.col_idx.size(), -1);
+        for (int i = 0; i < T->nbr; ++i) {
+            int q = U.row_ptr[i];
+            for (int a = T->h_row_ptr[i]; a < T->h_row_ptr[i + 1]; ++a) {
+                while (U.col_idx[q] != T->h_col_idx[a]) ++q;
+                src_of[q] = a;
+            }
+        }
+        gather_blocks(ctx, src_of, T, initv);
+        double* src = initv;
+        for (int d = 0; d < ndim; ++d) {
+            run_plan(ctx, per[d], b, b, opnd(G[d]), true, opnd(M), opnd(G[d]), src, A->val);
+            src = A->val;
+        }
+    } catch (...) {
+        dfree(initv);
+        delete A;
+        throw;
+    }
+    dfree(initv);
+    return A;
+}
+
+void construct_laplacian(mgldg_ctx* ctx, mgldg_ops* ops) {
+    MG_REQUIRE(ops->has_MGT(), MGLDG_ERR_ARG, "construct_laplacian needs M, G and T");
+    mgldg_bsr* A = laplacian(ctx, ops->M, ops->G, ops->ndim, ops->T);
+    delete ops->A;
+    ops->A = A;
+}
+
+// ------------------------------------------------------------ Galerkin -----
+// RATRAT (multigrid.h:115-157):
+//   M_c = T^T M_f T ; Minv = M_c(i,i)^-1 ; G_c,d = M_c^-1 T^T M_f G_f,d T ;
+//   T_c = T^T T_f T ; A_c = construct_laplacian(M_c, G_c, T_c)
+mgldg_ops* galerkin_ratrat(mgldg_ctx* ctx, const mgldg_ops* f, const mgldg_bsr* T) {
+    MG_REQUIRE(f->has_MGT(), MGLDG_ERR_ARG, "RATRAT needs M, G and T on the finer level");
+    MG_REQUIRE(T->nbr == f->M->nbr && T->br == f->M->br, MGLDG_ERR_SHAPE, "interpolation shape mismatch");
+    bsr_build_diag(f->M);
+    mgldg_ops* c = new mgldg_ops();
+    c->ctx = ctx;
+    c->ndim = f->ndim;
+    int* dstatus = nullptr;
+    double* minv = nullptr;
+    std::vector<mgldg_bsr*> tmp;
+    try {
+        const int bc = T->bc;
+        // coarse mass matrix (block diagonal): sum_k T(k,i)^T M(k,k) T(k,j)
+        std::vector<Plan> per;
+        Plan U = plan_triple({T}, f->M, nullptr, &per);
+        c->M = new_from_plan(ctx, U, bc, bc);
+        run_plan(ctx, per[0], bc, bc, opnd(T), true, opnd(f->M), opnd(T), nullptr, c->M->val);
+        bsr_build_diag(c->M);
+        // Minv: inverses of the diagonal blocks of M_c
+        dstatus = dalloc<int>(1);
+        MG_CHECK_CUDA(cudaMemsetAsync(dstatus, 0, sizeof(int), ctx->stream));
+        minv = dalloc<double>((size_t)c->M->nbr * bc * bc);
+        block_inverse(ctx, c->M, minv, dstatus);
+        check_status(ctx, dstatus, "coarse mass matrix");
+        for (int d = 0; d < f->ndim; ++d) {
+            mgldg_bsr* t1 = mm(ctx, f->G[d], false, T);   // G_f T
+            tmp.push_back(t1);
+            mgldg_bsr* t2 = mm(ctx, f->M, false, t1);     // M_f (G_f T)
+            tmp.push_back(t2);
+            mgldg_bsr* g = mm(ctx, T, true, t2);          // T^T M_f G_f T
+            tmp.push_back(g);
+            // G_c(i,j) = Minv_i G(i,j)
+            Plan P;
+            P.nbr = g->nbr; P.nbc = g->nbc;
+            P.row_ptr = g->h_row_ptr; P.col_idx = g->h_col_idx;
+            P.tptr.resize(g->nnzb + 1);
+            P.terms.resize(g->nnzb);
+            for (int i = 0; i < g->nbr; ++i)
+                for (int a = g->h_row_ptr[i]; a < g->h_row_ptr[i + 1]; ++a) {
+                    P.tptr[a] = a;
+                    P.terms[a] = Term{i, -1, a};
+                }
+            P.tptr[g->nnzb] = (int)g->nnzb;
+            c->G[d] = new_from_plan(ctx, P, bc, bc);
+            run_plan(ctx, P, bc, bc, Opnd{minv, nullptr, bc, bc}, false, Opnd{nullptr, nullptr, 0, 0}, opnd(g), nullptr,
+                     c->G[d]->val);
+            for (auto* m : tmp) delete m;
+            tmp.clear();
+        }
+        // T_c = T^T T_f T
+        mgldg_bsr* t1 = mm(ctx, f->T, false, T);
+        tmp.push_back(t1);
+        c->T = mm(ctx, T, true, t1);
+        for (auto* m : tmp) delete m;
+        tmp.clear();
+        c->A = laplacian(ctx, c->M, c->G, c->ndim, c->T);
+    } catch (...) {
+        for (auto* m : tmp) delete m;
+        dfree(dstatus);
+        dfree(minv);
+        delete c;
+        throw;
+    }
+    dfree(dstatus);
+    dfree(minv);
+    return c;
+}
+
+// RAT (multigrid.h:158-163): A_c = T^T A_f T
+mgldg_ops* galerkin_rat(mgldg_ctx* ctx, const mgldg_ops* f, const mgldg_bsr* T) {
+    MG_REQUIRE(f->A != nullptr, MGLDG_ERR_ARG, "RAT needs A on the finer level");
+    mgldg_ops* c = new mgldg_ops();
+    c->ctx = ctx;
+    c->ndim = f->ndim;
+    mgldg_bsr* t1 = nullptr;
+    try {
+        t1 = mm(ctx, f->A, false, T);
+        c->A = mm(ctx, T, true, t1);
+    } catch (...) {
+        delete t1;
+        delete c;
+        throw;
+    }
+    delete t1;
+    return c;
+}
+
+// -------------------------------------------------- dense coarsest inverse --
+__global__ void k_scatter_dense(int nbr, int b, const int* __restrict__ row_ptr, const int* __restrict__ col_idx,
+                                const double* __restrict__ val, const int* __restrict__ blk, int n, double* aug) {
+    // aug is n x 2n: [A | I]
+    for (int i = blockIdx.x; i < nbr; i += gridDim.x)
+        for (int k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
+            const double* a = val + (size_t)(blk ? blk[k] : k) * b * b;
+            int j = col_idx[k];
+            for (int q = threadIdx.x; q < b * b; q += blockDim.x) {
+                int r = q / b, c = q - r * b;
+                aug[(size_t)(i * b + r) * 2 * n + j * b + c] = a[q];
+            }
+        }
+}
+__global__ void k_identity_right(int n, double* aug) {
+    for (int r = blockIdx.x; r < n; r += gridDim.x)
+        for (int c = threadIdx.x; c < n; c += blockDim.x) aug[(size_t)r * 2 * n + n + c] = (r == c) ? 1.0 : 0.0;
+}
+
+// Gauss-Jordan on [A | I] with partial pivoting; one CTA of 1024 threads.
+__global__ void __launch_bounds__(1024) k_gauss_jordan(int n, double* aug, int* status) {
+    __shared__ double sv[32];
+    __shared__ int si[32];
+    __shared__ int piv;
+    __shared__ double pinv;
+    const int w2 = 2 * n;
+    for (int k = 0; k < n; ++k) {
+        double v = -1.0;
+        int idx = n;
+        for (int r = k + threadIdx.x; r < n; r += blockDim.x) {
+            double a = fabs(aug[(size_t)r * w2 + k]);
+            if (a > v) { v = a; idx = r; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            double v2 = __shfl_xor_sync(0xffffffffu, v, o);
+            int i2 = __shfl_xor_sync(0xffffffffu, idx, o);
+            if (v2 > v || (v2 == v && i2 < idx)) { v = v2; idx = i2; }
+        }
+        if ((threadIdx.x & 31) == 0) { sv[threadIdx.x >> 5] = v; si[threadIdx.x >> 5] = idx; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double bv = -1.0;
+            int bi = n;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+                if (sv[w] > bv || (sv[w] == bv && si[w] < bi)) { bv = sv[w]; bi = si[w]; }
+            if (!(bv > 0.0) || !isfinite(bv) || bi >= n) { *status = 1; bi = k; }
+            piv = bi;
+        }
+        __syncthreads();
+        const int p = piv;
+        if (p != k)
+            for (int c = threadIdx.x; c < w2; c += blockDim.x) {
+                double t = aug[(size_t)k * w2 + c];
+                aug[(size_t)k * w2 + c] = aug[(size_t)p * w2 + c];
+                aug[(size_t)p * w2 + c] = t;
+            }
+        __syncthreads();
+        if (threadIdx.x == 0) pinv = 1.0 / aug[(size_t)k * w2 + k];
+        __syncthreads();
+        for (int c = threadIdx.x; c < w2; c += blockDim.x) aug[(size_t)k * w2 + c] *= pinv;
+        __syncthreads();
+        // eliminate column k from every other row; the factors are read from
+        // column k before it is overwritten (column k is done last)
+        for (int q = threadIdx.x; q < n * w2; q += blockDim.x) {
+            int r = q / w2, c = q - r * w2;
+            if (r == k || c == k) continue;
+            aug[q] -= aug[(size_t)r * w2 + k] * aug[(size_t)k * w2 + c];
+        }
+        __syncthreads();
+        for (int r = threadIdx.x; r < n; r += blockDim.x)
+            if (r != k) aug[(size_t)r * w2 + k] = 0.0;
+        __syncthreads();
+    }
+}
+__global__ void k_extract_right(int n, const double* aug, double* out) {
+    for (int r = blockIdx.x; r < n; r += gridDim.x)
+        for (int c = threadIdx.x; c < n; c += blockDim.x) out[(size_t)r * n + c] = aug[(size_t)r * 2 * n + n + c];
+}
+
+void dense_spd_inverse(mgldg_ctx* ctx, const mgldg_bsr* A, double* out_inv) {
+    MG_REQUIRE(A->br == A->bc && A->nbr == A->nbc, MGLDG_ERR_SHAPE, "coarse matrix must be square");
+    const int n = A->nbr * A->br;
+    MG_REQUIRE(n <= 4096, MGLDG_ERR_UNSUPPORTED, "dense coarsest solve limited to 4096 unknowns");
+    double* aug = nullptr;
+    int* dstatus = nullptr;
+    try {
+        aug = dalloc<double>((size_t)n * 2 * n);
+        dstatus = dalloc<int>(1);
+        MG_CHECK_CUDA(cudaMemsetAsync(aug, 0, (size_t)n * 2 * n * sizeof(double), ctx->stream));
+        MG_CHECK_CUDA(cudaMemsetAsync(dstatus, 0, sizeof(int), ctx->stream));
+        {
+            Launch L(ctx, MGLDG_K_SETUP);
+            k_scatter_dense<<<std::min(A->nbr, 1024), 256, 0, ctx->stream>>>(A->nbr, A->br, A->row_ptr, A->col_idx,
+                                                                             A->val, A->blk, n, aug);
+        }
+        {
+            Launch L(ctx, MGLDG_K_SETUP);
+            k_identity_right<<<std::min(n, 1024), 256, 0, ctx->stream>>>(n, aug);
+        }
+        {
+            Launch L(ctx, MGLDG_K_SETUP);
+            k_gauss_jordan<<<1, 1024, 0, ctx->stream>>>(n, aug, dstatus);
+        }
+        {
+            Launch L(ctx, MGLDG_K_SETUP);
+            k_extract_right<<<std::min(n, 1024), 256, 0, ctx->stream>>>(n, aug, out_inv);
+        }
+        check_launch();
+        int h = 0;
+        download(ctx, &h, dstatus, 1);
+        sync(ctx);
+        MG_REQUIRE(h == 0, MGLDG_ERR_NOT_SPD, "coarsest-level matrix is singular");
+    } catch (...) {
+        dfree(aug);
+        dfree(dstatus);
+        throw;
+    }
+    dfree(aug);
+    dfree(dstatus);
+}
+
+}  // namespace mg
+
+mgldg_ops::~mgldg_ops() {
+    delete M;
+    for (auto* g : G) delete g;
+    delete T;
+    delete A;
+}
+
+// ================================================================== C ABI ==
+extern "C" int mgldg_ops_create(mgldg_ctx* ctx, int ndim, mgldg_bsr* M, mgldg_bsr* const* G, mgldg_bsr* T,
+                                mgldg_ops** out) {
+    MG_API_BEGIN(ctx)
+    MG_REQUIRE(out && M && G && T && ndim >= 1 && ndim <= 3, MGLDG_ERR_ARG, "bad operator arguments");
+    *out = nullptr;
+    const int b = M->br;
+    MG_REQUIRE(M->bc == b && T->br == b && T->bc == b && M->nbr == M->nbc && T->nbr == M->nbr && T->nbc == M->nbr,
+               MGLDG_ERR_SHAPE, "M and T must be square with equal blocks");
+    for (int d = 0; d < ndim; ++d) {
+        MG_REQUIRE(G[d] != nullptr, MGLDG_ERR_ARG, "null gradient");
+        MG_REQUIRE(G[d]->br == b && G[d]->bc == b && G[d]->nbr == M->nbr && G[d]->nbc == M->nbr, MGLDG_ERR_SHAPE,
+                   "gradient shape mismatch");
+    }
+    mgldg_ops* o = new mgldg_ops();
+    o->ctx = ctx;
+    o->ndim = ndim;
+    o->M = M;
+    for (int d = 0; d < ndim; ++d) o->G[d] = G[d];
+    o->T = T;
+    *out = o;
+    MG_API_END
+}
+
+extern "C" int mgldg_ops_create_A(mgldg_ctx* ctx, mgldg_bsr* A, mgldg_ops** out) {
+    MG_API_BEGIN(ctx)
+    MG_REQUIRE(out && A, MGLDG_ERR_ARG, "bad operator arguments");
+    MG_REQUIRE(A->br == A->bc && A->nbr == A->nbc, MGLDG_ERR_SHAPE, "A must be square");
+    mgldg_ops* o = new mgldg_ops();
+    o->ctx = ctx;
+    o->ndim = 0;
+    o->A = A;
+    *out = o;
+    MG_API_END
+}
+
+extern "C" int mgldg_ops_construct_laplacian(mgldg_ctx* ctx, mgldg_ops* ops) {
+    MG_API_BEGIN(ctx)
+    MG_REQUIRE(ops != nullptr, MGLDG_ERR_ARG, "null operators");
+    construct_laplacian(ctx, ops);
+    MG_API_END
+}
+
+extern "C" int mgldg_ops_get(const mgldg_ops* ops, int which, const mgldg_bsr** A) {
+    if (!ops || !A) return MGLDG_ERR_ARG;
+    switch (which) {
+        case 0: *A = ops->M; break;
+        case 1: *A = ops->G[0]; break;
+        case 2: *A = ops->G[1]; break;
+        case 3: *A = ops->T; break;
+        case 4: *A = ops->A; break;
+        default: return MGLDG_ERR_ARG;
+    }
+    return *A ? MGLDG_OK : MGLDG_ERR_ARG;
+}
+
+extern "C" int mgldg_ops_destroy(mgldg_ops* ops) {
+    if (!ops) return MGLDG_OK;
+    if (ops->ctx) cudaSetDevice(ops->ctx->device);
+    delete ops;
+    return MGLDG_OK;
+}

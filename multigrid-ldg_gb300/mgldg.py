@@ -1,0 +1,386 @@
+"""Python host mirror of the reference's solver interface over the libmgldg C ABI.
+
+The names follow danfortunato/multigrid-ldg: SparseBlockMatrix
+(src/cartesian/util/sparseblockmatrix.h:62-165), LDGOperators
+(src/cartesian/dg/ldgpoisson.h:15-53), MG parameters and Multigrid
+(src/cartesian/multigrid/multigrid.h:48-62, 280-433) and pcg
+(src/cartesian/multigrid/krylov.h:22-82).  Every call goes through the
+C-ABI library libmgldg.so (CUDA, sm_103a); there is no CPU fallback: if the
+library or a GPU is missing, the calls raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmgldg.so")
+
+OK, ERR_ARG, ERR_SHAPE, ERR_CUDA, ERR_BREAKDOWN, ERR_TIMEOUT, ERR_NOT_SPD, ERR_NOMEM, ERR_UNSUPPORTED = range(9)
+RELAX_JACOBI, RELAX_GAUSS_SEIDEL = 0, 1
+COARSE_CHOLESKY, COARSE_RELAXATION, COARSE_DENSE = 0, 1, 2
+RESTRICT_RAT, RESTRICT_RATRAT = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+K_SPMV, K_GS, K_JACOBI, K_TRANSFER, K_COARSE, K_VECTOR, K_SETUP = range(7)
+K_NAMES = ["spmv", "gauss_seidel", "jacobi", "transfer", "coarse", "vector", "setup"]
+
+# every symbol declared in include/mgldg.h
+EXPORTS = [
+    "mgldg_ctx_create", "mgldg_ctx_destroy", "mgldg_last_error", "mgldg_ctx_sync", "mgldg_ctx_stream",
+    "mgldg_master_tables", "mgldg_bsr_create", "mgldg_bsr_destroy", "mgldg_bsr_info", "mgldg_bsr_download",
+    "mgldg_bsr_mv", "mgldg_bsr_mv_dev", "mgldg_bsr_mv_t", "mgldg_ops_create", "mgldg_ops_create_A",
+    "mgldg_ops_construct_laplacian", "mgldg_ops_get", "mgldg_ops_destroy", "mgldg_mg_params_default",
+    "mgldg_mg_create", "mgldg_mg_destroy", "mgldg_mg_nlevels", "mgldg_mg_level_op", "mgldg_mg_vcycle",
+    "mgldg_mg_vcycle_dev", "mgldg_mg_relax", "mgldg_pcg", "mgldg_pcg_dev", "mgldg_cartesian_create",
+    "mgldg_problem_destroy", "mgldg_problem_info", "mgldg_problem_ops", "mgldg_problem_interp",
+    "mgldg_problem_rhs_gaussian", "mgldg_problem_rhs_gaussian_dev", "mgldg_prof_enable", "mgldg_prof_reset",
+    "mgldg_prof_query", "mgldg_gs_levels", "mgldg_selftest_wait_timeout",
+]
+
+
+def gs_levels(row_ptr, col_idx, reverse=False):
+    """Host-side level schedule of a Gauss-Seidel sweep: (level per row, rows in level order, nlevels)."""
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int32)
+    ci = np.ascontiguousarray(col_idx, dtype=np.int32)
+    if len(ci) == 0:
+        ci = np.zeros(1, np.int32)
+    n = len(rp) - 1
+    lev = np.zeros(max(1, n), np.int32)
+    order = np.zeros(max(1, n), np.int32)
+    nl = C.c_int()
+    rc = lib().mgldg_gs_levels(n, rp, ci, int(reverse), lev, order, C.byref(nl))
+    if rc:
+        raise MgldgError(rc, "gs_levels")
+    return lev[:n], order[:n], nl.value
+
+
+class MgldgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"libmgldg error {code}: {msg}")
+        self.code = code
+
+
+class MGParams(C.Structure):
+    """MG::Parameters (multigrid.h:48-62) plus precision / level-count / mean-projection."""
+    _fields_ = [("relaxation", C.c_int), ("omega", C.c_double), ("solver", C.c_int), ("npre", C.c_int),
+                ("npost", C.c_int), ("restriction", C.c_int), ("precision", C.c_int), ("max_levels", C.c_int),
+                ("mean_project", C.c_int)]
+
+
+_lib = None
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+def lib():
+    """Loads libmgldg.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run multigrid-ldg_gb300/build.py")
+        L = C.CDLL(LIB_PATH)
+        vp, pvp = C.c_void_p, C.POINTER(C.c_void_p)
+        i64p = C.POINTER(C.c_int64)
+        ip = C.POINTER(C.c_int)
+        L.mgldg_ctx_create.argtypes = [C.c_int, pvp]
+        L.mgldg_ctx_destroy.argtypes = [vp]
+        L.mgldg_last_error.argtypes = [vp]
+        L.mgldg_last_error.restype = C.c_char_p
+        L.mgldg_ctx_sync.argtypes = [vp]
+        L.mgldg_ctx_stream.argtypes = [vp]
+        L.mgldg_ctx_stream.restype = C.c_void_p
+        L.mgldg_master_tables.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.mgldg_bsr_create.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, _ip, _ip, _dp, pvp]
+        L.mgldg_bsr_destroy.argtypes = [vp]
+        L.mgldg_bsr_info.argtypes = [vp, ip, ip, ip, ip, i64p]
+        L.mgldg_bsr_download.argtypes = [vp, vp, _ip, _ip, _dp]
+        L.mgldg_bsr_mv.argtypes = [vp, C.c_double, vp, _dp, C.c_double, _dp]
+        L.mgldg_bsr_mv_dev.argtypes = [vp, C.c_double, vp, vp, C.c_double, vp]
+        L.mgldg_bsr_mv_t.argtypes = [vp, vp, _dp, _dp]
+        L.mgldg_ops_create.argtypes = [vp, C.c_int, vp, C.POINTER(C.c_void_p), vp, pvp]
+        L.mgldg_ops_create_A.argtypes = [vp, vp, pvp]
+        L.mgldg_ops_construct_laplacian.argtypes = [vp, vp]
+        L.mgldg_ops_get.argtypes = [vp, C.c_int, pvp]
+        L.mgldg_ops_destroy.argtypes = [vp]
+        L.mgldg_mg_params_default.argtypes = [C.POINTER(MGParams)]
+        L.mgldg_mg_params_default.restype = None
+        L.mgldg_mg_create.argtypes = [vp, vp, C.POINTER(C.c_void_p), C.c_int, C.POINTER(MGParams), pvp]
+        L.mgldg_mg_destroy.argtypes = [vp]
+        L.mgldg_mg_nlevels.argtypes = [vp, ip]
+        L.mgldg_mg_level_op.argtypes = [vp, C.c_int, C.c_int, pvp]
+        L.mgldg_mg_vcycle.argtypes = [vp, vp, _dp, _dp]
+        L.mgldg_mg_vcycle_dev.argtypes = [vp, vp, vp, vp]
+        L.mgldg_mg_relax.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, _dp, _dp]
+        L.mgldg_pcg.argtypes = [vp, vp, vp, _dp, _dp, C.c_double, C.c_int, ip, _dp]
+        L.mgldg_pcg_dev.argtypes = [vp, vp, vp, vp, vp, C.c_double, C.c_int, ip, _dp]
+        L.mgldg_cartesian_create.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_double, pvp]
+        L.mgldg_problem_destroy.argtypes = [vp]
+        L.mgldg_problem_info.argtypes = [vp, ip, ip, i64p, ip]
+        L.mgldg_problem_ops.argtypes = [vp, pvp]
+        L.mgldg_problem_interp.argtypes = [vp, C.c_int, pvp]
+        L.mgldg_problem_rhs_gaussian.argtypes = [vp, vp, C.c_uint64, _dp]
+        L.mgldg_problem_rhs_gaussian_dev.argtypes = [vp, vp, C.c_uint64, vp]
+        L.mgldg_prof_enable.argtypes = [vp, C.c_int]
+        L.mgldg_prof_reset.argtypes = [vp]
+        L.mgldg_prof_query.argtypes = [vp, C.c_int, i64p, C.POINTER(C.c_double)]
+        L.mgldg_gs_levels.argtypes = [C.c_int, _ip, _ip, C.c_int, _ip, _ip, ip]
+        L.mgldg_selftest_wait_timeout.argtypes = [vp, C.c_int64, ip]
+        _lib = L
+    return _lib
+
+
+def master_tables(P):
+    """Reference-element tables compiled into the library (master.h:147-214)."""
+    out = [np.zeros(P), np.zeros(P), np.zeros(P * P), np.zeros(P * P), np.zeros(P * P), np.zeros(10), np.zeros(10)]
+    rc = lib().mgldg_master_tables(P, *out)
+    if rc:
+        raise MgldgError(rc, "master_tables")
+    nodes, denom, mass, invmass, diff, qx, qw = out
+    return dict(nodes=nodes, denom=denom, mass=mass.reshape(P, P), invmass=invmass.reshape(P, P),
+                diff=diff.reshape(P, P), quad_x=qx, quad_w=qw)
+
+
+class Context:
+    """One GPU and one CUDA stream (mgldg_ctx)."""
+
+    def __init__(self, device=0):
+        h = C.c_void_p()
+        rc = lib().mgldg_ctx_create(device, C.byref(h))
+        if rc:
+            raise MgldgError(rc, f"cannot create a context on device {device}")
+        self.h = h
+
+    def check(self, rc, what=""):
+        if rc:
+            raise MgldgError(rc, f"{what}: {lib().mgldg_last_error(self.h).decode()}")
+
+    def sync(self):
+        self.check(lib().mgldg_ctx_sync(self.h), "sync")
+
+    @property
+    def stream(self):
+        return lib().mgldg_ctx_stream(self.h)
+
+    def prof_enable(self, on=True):
+        self.check(lib().mgldg_prof_enable(self.h, int(on)), "prof_enable")
+
+    def prof_reset(self):
+        self.check(lib().mgldg_prof_reset(self.h), "prof_reset")
+
+    def prof(self):
+        out = {}
+        for k, name in enumerate(K_NAMES):
+            n, ms = C.c_int64(), C.c_double()
+            self.check(lib().mgldg_prof_query(self.h, k, C.byref(n), C.byref(ms)), "prof_query")
+            out[name] = (n.value, ms.value)
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mgldg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class SparseBlockMatrix:
+    """Block-CSR matrix on the GPU (SparseBlockMatrix<P,Q>)."""
+
+    def __init__(self, ctx, handle, owned=True):
+        self.ctx, self.h, self.owned = ctx, handle, owned
+
+    @classmethod
+    def from_csr(cls, ctx, nbr, nbc, br, bc, row_ptr, col_idx, vals):
+        h = C.c_void_p()
+        rp = np.ascontiguousarray(row_ptr, dtype=np.int32)
+        ci = np.ascontiguousarray(col_idx, dtype=np.int32)
+        v = np.ascontiguousarray(vals, dtype=np.float64).ravel()
+        if len(ci) == 0:
+            ci = np.zeros(1, np.int32)
+            v = np.zeros(1)
+        ctx.check(lib().mgldg_bsr_create(ctx.h, nbr, nbc, br, bc, rp, ci, v, C.byref(h)), "bsr_create")
+        return cls(ctx, h)
+
+    def info(self):
+        a = [C.c_int() for _ in range(4)]
+        nnzb = C.c_int64()
+        self.ctx.check(lib().mgldg_bsr_info(self.h, *[C.byref(x) for x in a], C.byref(nnzb)), "bsr_info")
+        return tuple(x.value for x in a) + (nnzb.value,)
+
+    def download(self):
+        nbr, nbc, br, bc, nnzb = self.info()
+        rp = np.zeros(nbr + 1, np.int32)
+        ci = np.zeros(max(1, nnzb), np.int32)
+        v = np.zeros(max(1, nnzb * br * bc))
+        self.ctx.check(lib().mgldg_bsr_download(self.ctx.h, self.h, rp, ci, v), "bsr_download")
+        return rp, ci[:nnzb], v[:nnzb * br * bc].reshape(nnzb, br, bc)
+
+    def mv(self, x, alpha=1.0, beta=0.0, y=None):
+        nbr, nbc, br, bc, _ = self.info()
+        y = np.zeros(nbr * br) if y is None else np.array(y, dtype=np.float64)
+        self.ctx.check(lib().mgldg_bsr_mv(self.ctx.h, alpha, self.h, np.ascontiguousarray(x, np.float64), beta, y),
+                       "bsr_mv")
+        return y
+
+    def mv_t(self, x):
+        nbr, nbc, br, bc, _ = self.info()
+        y = np.zeros(nbc * bc)
+        self.ctx.check(lib().mgldg_bsr_mv_t(self.ctx.h, self.h, np.ascontiguousarray(x, np.float64), y), "bsr_mv_t")
+        return y
+
+    def release(self):
+        """Gives up ownership (the C side took it)."""
+        self.owned = False
+        return self.h
+
+    def __del__(self):
+        if getattr(self, "owned", False) and self.h:
+            try:
+                lib().mgldg_bsr_destroy(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+
+class LDGOperators:
+    """LDGOperators<N,P>{M, G[N], T, A} (ldgpoisson.h:15-53)."""
+
+    def __init__(self, ctx, handle, owned=True, keep=None):
+        self.ctx, self.h, self.owned, self._keep = ctx, handle, owned, keep
+
+    @classmethod
+    def create(cls, ctx, M, G, T):
+        h = C.c_void_p()
+        arr = (C.c_void_p * len(G))(*[g.h for g in G])
+        ctx.check(lib().mgldg_ops_create(ctx.h, len(G), M.h, arr, T.h, C.byref(h)), "ops_create")
+        for m in [M, T] + list(G):
+            m.release()
+        return cls(ctx, h)
+
+    @classmethod
+    def create_A(cls, ctx, A):
+        h = C.c_void_p()
+        ctx.check(lib().mgldg_ops_create_A(ctx.h, A.h, C.byref(h)), "ops_create_A")
+        A.release()
+        return cls(ctx, h)
+
+    def construct_laplacian(self):
+        self.ctx.check(lib().mgldg_ops_construct_laplacian(self.ctx.h, self.h), "construct_laplacian")
+
+    def get(self, which):
+        out = C.c_void_p()
+        self.ctx.check(lib().mgldg_ops_get(self.h, which, C.byref(out)), "ops_get")
+        return SparseBlockMatrix(self.ctx, out, owned=False)
+
+    @property
+    def A(self):
+        return self.get(4)
+
+    def __del__(self):
+        if getattr(self, "owned", False) and self.h:
+            try:
+                lib().mgldg_ops_destroy(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+
+def mg_params(**kw):
+    p = MGParams()
+    lib().mgldg_mg_params_default(C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
+class Multigrid:
+    """Multigrid<N,P>(ops, hierarchy, params) (multigrid.h:291-301)."""
+
+    def __init__(self, ctx, ops, T, **params):
+        self.ctx, self.ops = ctx, ops
+        self.params = mg_params(**params)
+        arr = (C.c_void_p * max(1, len(T)))(*[t.h for t in T])
+        h = C.c_void_p()
+        ctx.check(lib().mgldg_mg_create(ctx.h, ops.h, arr, len(T), C.byref(self.params), C.byref(h)), "mg_create")
+        self.h = h
+        n = C.c_int()
+        ctx.check(lib().mgldg_mg_nlevels(h, C.byref(n)), "mg_nlevels")
+        self.nlevels = n.value
+
+    def level_op(self, level, which):
+        out = C.c_void_p()
+        self.ctx.check(lib().mgldg_mg_level_op(self.h, level, which, C.byref(out)), "level_op")
+        return SparseBlockMatrix(self.ctx, out, owned=False)
+
+    def vcycle(self, b, x=None):
+        b = np.ascontiguousarray(b, np.float64)
+        x = np.zeros_like(b) if x is None else np.array(x, dtype=np.float64)
+        self.ctx.check(lib().mgldg_mg_vcycle(self.ctx.h, self.h, b, x), "vcycle")
+        return x
+
+    def relax(self, level, n, reverse, b, x):
+        x = np.array(x, dtype=np.float64)
+        self.ctx.check(lib().mgldg_mg_relax(self.ctx.h, self.h, level, n, int(reverse),
+                                            np.ascontiguousarray(b, np.float64), x), "relax")
+        return x
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            try:
+                lib().mgldg_mg_destroy(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+
+def pcg(ctx, A, b, x=None, precon=None, tol=1e-8, maxit=200):
+    """pcg(A, b, x, precon, tol, maxit) (krylov.h:22-68); returns (x, residual history)."""
+    b = np.ascontiguousarray(b, np.float64)
+    x = np.zeros_like(b) if x is None else np.array(x, dtype=np.float64)
+    hist = np.zeros(max(1, maxit))
+    it = C.c_int()
+    rc = lib().mgldg_pcg(ctx.h, precon.h if precon is not None else None, A.h, b, x, tol, maxit, C.byref(it), hist)
+    ctx.check(rc, "pcg")
+    return x, hist[:it.value].copy()
+
+
+class CartesianProblem:
+    """Uniform n x n quadtree mesh, Q_{P-1} LDG operators and hierarchy, built on the GPU."""
+
+    def __init__(self, ctx, P, n, tau0=None, tauD=None):
+        tau0 = float(n) if tau0 is None else tau0
+        tauD = float(n) if tauD is None else tauD
+        h = C.c_void_p()
+        ctx.check(lib().mgldg_cartesian_create(ctx.h, P, n, tau0, tauD, C.byref(h)), "cartesian_create")
+        self.ctx, self.h = ctx, h
+        ne, npl, nT = C.c_int(), C.c_int(), C.c_int()
+        ndof = C.c_int64()
+        ctx.check(lib().mgldg_problem_info(h, C.byref(ne), C.byref(npl), C.byref(ndof), C.byref(nT)), "info")
+        self.ne, self.npl, self.ndof, self.nT = ne.value, npl.value, ndof.value, nT.value
+        o = C.c_void_p()
+        ctx.check(lib().mgldg_problem_ops(h, C.byref(o)), "problem_ops")
+        self.ops = LDGOperators(ctx, o, owned=False, keep=self)
+        self.T = []
+        for l in range(self.nT):
+            t = C.c_void_p()
+            ctx.check(lib().mgldg_problem_interp(h, l, C.byref(t)), "problem_interp")
+            self.T.append(SparseBlockMatrix(ctx, t, owned=False))
+
+    def rhs_gaussian(self, seed):
+        b = np.zeros(self.ndof)
+        self.ctx.check(lib().mgldg_problem_rhs_gaussian(self.ctx.h, self.h, seed, b), "rhs_gaussian")
+        return b
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            try:
+                lib().mgldg_problem_destroy(self.h)
+            except Exception:
+                pass
+            self.h = None
