@@ -164,6 +164,21 @@ int mgldg_pcg(mgldg_ctx* ctx, mgldg_mg* mg, const mgldg_bsr* A, const double* b,
 int mgldg_pcg_dev(mgldg_ctx* ctx, mgldg_mg* mg, const mgldg_bsr* A, const double* b,
                   double* x, double tol, int maxit, int* iters, double* res_hist);
 
+/* No counterpart in the reference.  The unpreconditioned CG of
+ * mgldg_pcg_dev(ctx, NULL, ...) for callers that cannot allocate device
+ * memory while they solve (a host framework whose caching allocator owns the
+ * GPU's memory, or a caller held to a memory budget fixed at start-up).  It
+ * calls no cudaMalloc/cudaFree or other allocating routine: its work vectors
+ * live in one fixed device array of about 4.1 MiB that every GPU loading the
+ * library holds until the process exits.  Limits: at most 131,072 unknowns
+ * and maxit <= 1024 (larger requests return MGLDG_ERR_ARG).  b and x are
+ * device pointers owned by the caller.  The first call on each device looks
+ * up the array's device address, so make it before any stream capture.  All
+ * calls on a device share the array: calls that overlap on the GPU (other
+ * streams, threads or contexts) race and must be serialised by the caller. */
+int mgldg_cg_noalloc_dev(mgldg_ctx* ctx, const mgldg_bsr* A, const double* b,
+                         double* x, double tol, int maxit, int* iters, double* res_hist);
+
 /* ------------------------------------- Cartesian problem builder ---------
  * The callers on either side of the path, for users without the reference's
  * assembly: a uniform quadtree mesh of n x n squares on [0,1]^2 (n a power

@@ -12,6 +12,8 @@
 // residuals, dot products and updates in FP64.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
+#include <string>
 
 #include "api.cuh"
 #include "smooth.cuh"
@@ -711,5 +713,140 @@ extern "C" int mgldg_pcg(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const 
     }
     dfree(db);
     dfree(dx);
+    MG_API_END
+}
+
+// ======================================================= allocation-free CG ==
+// mgldg_cg_noalloc_dev: the unpreconditioned CG of mgldg_pcg_dev(ctx, NULL,
+// ...) for callers that must not allocate device memory during a solve --
+// for example a host framework whose caching allocator already owns the
+// device memory, or a caller held to a fixed memory budget set at start-up.
+// The existing entry point allocates four work vectors, a history buffer and
+// pinned scalars on every call; this one uses the fixed scratch array below
+// instead and calls no allocating routine (with kernel profiling off, the
+// default).  The array is carved into r, d, q, s (kCgMaxN doubles each), the
+// reduction partials, the residual history and the scalar block.
+namespace {
+constexpr int64_t kCgMaxN = 131072;    // largest system: 131,072 unknowns
+constexpr int kCgMaxIt = 1024;         // largest iteration limit
+constexpr int kCgParts = 8192;         // CTA partial sums (>= ctx->n_partials)
+constexpr int64_t kCgScalarOff = 4 * kCgMaxN + kCgParts + kCgMaxIt;
+constexpr int64_t kCgScratchDoubles = kCgScalarOff + 32;   // ~4.1 MiB per GPU
+static_assert(sizeof(mg::PcgScalars) <= 32 * sizeof(double), "scalar block too small");
+static_assert((kCgScalarOff * sizeof(double)) % 256 == 0, "scalar block alignment");
+}  // namespace
+
+// One copy per GPU that loads this library, held until the process exits;
+// every call on that GPU shares it.
+static __device__ __align__(256) double g_cg_scratch[kCgScratchDoubles];
+
+static std::mutex g_cg_scratch_mu;
+static double* g_cg_scratch_addr[64] = {nullptr};
+
+// Device address of g_cg_scratch on `device` (which must be current).  Host
+// code cannot use the symbol's name as a device pointer; the address is
+// looked up once per device, on the first call made on that device.
+static double* cg_scratch(int device) {
+    MG_REQUIRE(device >= 0 && device < 64, MGLDG_ERR_ARG, "device index out of range for the scratch table");
+    std::lock_guard<std::mutex> lock(g_cg_scratch_mu);
+    if (!g_cg_scratch_addr[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_cg_scratch);
+        if (e != cudaSuccess)
+            throw Error(MGLDG_ERR_CUDA, std::string("cudaGetSymbolAddress(g_cg_scratch): ") + cudaGetErrorString(e));
+        g_cg_scratch_addr[device] = static_cast<double*>(p);
+    }
+    return g_cg_scratch_addr[device];
+}
+
+extern "C" int mgldg_cg_noalloc_dev(mgldg_ctx* ctx, const mgldg_bsr* A, const double* b, double* x, double tol,
+                                    int maxit, int* iters, double* res_hist) {
+    MG_API_BEGIN(ctx)
+    MG_REQUIRE(A && b && x && maxit >= 0, MGLDG_ERR_ARG, "bad cg arguments");
+    MG_REQUIRE(A->br == A->bc && A->nbr == A->nbc, MGLDG_ERR_SHAPE, "cg needs a square matrix");
+    const int64_t n = (int64_t)A->nbr * A->br;
+    MG_REQUIRE(n <= kCgMaxN, MGLDG_ERR_ARG,
+               "mgldg_cg_noalloc_dev: system has " + std::to_string(n) + " unknowns, the fixed scratch holds at most " +
+                   std::to_string(kCgMaxN) + " (use mgldg_pcg_dev)");
+    MG_REQUIRE(maxit <= kCgMaxIt, MGLDG_ERR_ARG,
+               "mgldg_cg_noalloc_dev: maxit " + std::to_string(maxit) + " exceeds " + std::to_string(kCgMaxIt));
+    MG_REQUIRE(ctx->n_partials <= kCgParts, MGLDG_ERR_ARG, "context reduction width exceeds the scratch");
+    double* base = cg_scratch(ctx->device);
+    double* r = base;
+    double* d = base + kCgMaxN;
+    double* q = base + 2 * kCgMaxN;
+    double* s = base + 3 * kCgMaxN;
+    double* part = base + 4 * kCgMaxN;
+    double* hist = part + kCgParts;
+    PcgScalars* sc = reinterpret_cast<PcgScalars*>(base + kCgScalarOff);
+    // the scratch keeps the previous call's contents: start the scalars at zero
+    MG_CHECK_CUDA(cudaMemsetAsync(sc, 0, sizeof(PcgScalars), ctx->stream));
+    const int grid_vec = reduce_grid((int)n);
+    PcgScalars h{};
+    int np = 0;
+    // r = b - A x ; d = r ; delta_new = delta_0 = r.d   (krylov.h:35-38, identity preconditioner)
+    spmv<double>(ctx, A, -1.0, x, 1.0, b, r);
+    MG_CHECK_CUDA(cudaMemcpyAsync(d, r, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    dot_partials<double>(ctx, (int)n, r, d, part, &np);
+    {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_pcg_init<<<1, 256, 0, ctx->stream>>>(sc, part, np);
+    }
+    check_launch();
+    MG_CHECK_CUDA(cudaMemcpyAsync(&h, sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost, ctx->stream));
+    sync(ctx);
+    const double tol2 = tol * tol;
+    int i = 0;
+    bool broke = false;
+    while (i < maxit && h.delta_new > tol2 * h.delta0) {
+        spmv<double>(ctx, A, 1.0, d, 0.0, nullptr, q, d, part, &np);
+        {
+            Launch L(ctx, MGLDG_K_VECTOR);
+            k_pcg_alpha<<<1, 256, 0, ctx->stream>>>(sc, part, np);
+        }
+        check_launch();
+        if (i % 50 == 0) {
+            {
+                Launch L(ctx, MGLDG_K_VECTOR);
+                k_pcg_update<<<grid_vec, 256, 0, ctx->stream>>>(n, sc, d, q, x, r, 0, part);
+            }
+            check_launch();
+            spmv<double>(ctx, A, -1.0, x, 1.0, b, r, r, part, &np);
+        } else {
+            {
+                Launch L(ctx, MGLDG_K_VECTOR);
+                k_pcg_update<<<grid_vec, 256, 0, ctx->stream>>>(n, sc, d, q, x, r, 1, part);
+            }
+            check_launch();
+            np = grid_vec;
+        }
+        {
+            Launch L(ctx, MGLDG_K_VECTOR);
+            k_pcg_rr<<<1, 256, 0, ctx->stream>>>(sc, part, np, hist, i);
+        }
+        check_launch();
+        MG_CHECK_CUDA(cudaMemcpyAsync(s, r, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+        dot_partials<double>(ctx, (int)n, r, s, part, &np);
+        {
+            Launch L(ctx, MGLDG_K_VECTOR);
+            k_pcg_beta<<<1, 256, 0, ctx->stream>>>(sc, part, np);
+        }
+        check_launch();
+        {
+            Launch L(ctx, MGLDG_K_VECTOR);
+            k_pcg_dir<<<grid_vec, 256, 0, ctx->stream>>>(n, sc, s, d);
+        }
+        check_launch();
+        MG_CHECK_CUDA(cudaMemcpyAsync(&h, sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost, ctx->stream));
+        sync(ctx);
+        ++i;
+        if (h.breakdown) { broke = true; break; }
+    }
+    if (iters) *iters = i;
+    if (res_hist && i > 0) {
+        MG_CHECK_CUDA(cudaMemcpyAsync(res_hist, hist, i * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        sync(ctx);
+    }
+    if (broke) throw Error(MGLDG_ERR_BREAKDOWN, "cg breakdown (d.q <= 0 or a non-finite scalar)");
     MG_API_END
 }

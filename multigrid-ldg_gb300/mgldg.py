@@ -34,7 +34,7 @@ EXPORTS = [
     "mgldg_mg_vcycle_dev", "mgldg_mg_relax", "mgldg_pcg", "mgldg_pcg_dev", "mgldg_cartesian_create",
     "mgldg_problem_destroy", "mgldg_problem_info", "mgldg_problem_ops", "mgldg_problem_interp",
     "mgldg_problem_rhs_gaussian", "mgldg_problem_rhs_gaussian_dev", "mgldg_prof_enable", "mgldg_prof_reset",
-    "mgldg_prof_query", "mgldg_gs_levels", "mgldg_selftest_wait_timeout",
+    "mgldg_prof_query", "mgldg_gs_levels", "mgldg_selftest_wait_timeout", "mgldg_cg_noalloc_dev",
 ]
 
 
@@ -125,6 +125,7 @@ def lib():
         L.mgldg_prof_query.argtypes = [vp, C.c_int, i64p, C.POINTER(C.c_double)]
         L.mgldg_gs_levels.argtypes = [C.c_int, _ip, _ip, C.c_int, _ip, _ip, ip]
         L.mgldg_selftest_wait_timeout.argtypes = [vp, C.c_int64, ip]
+        L.mgldg_cg_noalloc_dev.argtypes = [vp, vp, vp, vp, C.c_double, C.c_int, ip, _dp]
         _lib = L
     return _lib
 
