@@ -14,8 +14,8 @@ counts grow with n); the parity tests keep the projection on.
 
 One step = one MG-PCG solve from x = 0 with b already in HBM.  The headline
 value is the mixed form (FP32 V-cycle, FP64 CG and coarsest solve) with
-block Gauss-Seidel; the plain FP64 form and the damped block-Jacobi
-(omega = 0.7) variants are timed beside it.  The operator (2.68 GB in FP64)
+damped block Jacobi (omega = 0.7), the fastest form; the plain FP64 form and
+the block Gauss-Seidel (omega = 0.8) variants are timed beside it.  The operator (2.68 GB in FP64)
 is larger than L2, so no flush is needed between steps.
 
 --impl reference times the CPU oracle (the restatement of the reference's
@@ -174,6 +174,42 @@ def level_bytes(mg, nlev, s):
     return out
 
 
+FORMS = {
+    # name: (relaxation, omega, precision) -- MGLDG_RELAX_* / MGLDG_PREC_* values
+    "mixed_jacobi": (0, 0.7, 1),
+    "fp64_jacobi": (0, 0.7, 0),
+    "mixed_gs": (1, 0.8, 1),
+    "fp64_gs": (1, 0.8, 0),
+}
+FORM_TEXT = {"mixed_jacobi": "mixed precision, damped block Jacobi omega=0.7",
+             "fp64_jacobi": "FP64, damped block Jacobi omega=0.7",
+             "mixed_gs": "mixed precision, block Gauss-Seidel omega=0.8",
+             "fp64_gs": "FP64, block Gauss-Seidel omega=0.8"}
+# FP64 Gauss-Seidel MG-PCG iterations of the default workload (measured on
+# the GPU; the oracle runs the same algorithm) -- used by the reference arm,
+# which only samples the first iteration
+REF_ITERS = 16
+
+
+def fp64_peak_tflops(torch):
+    """cuBLAS FP64 GEMM rate (the FP64 ceiling of this GPU), best of 3."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    bm = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    a @ bm
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        a @ bm
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, bm
+    return 2 * n ** 3 / (best * 1e-3) / 1e12
+
+
 def run_gpu(args, ws, rank, local):
     import torch
     import mgldg
@@ -192,82 +228,86 @@ def run_gpu(args, ws, rank, local):
     ctx.check(L.mgldg_problem_rhs_gaussian_dev(ctx.h, prob.h, WL["seed"], C.c_void_p(b.data_ptr())), "rhs")
     ctx.sync()
     A = prob.ops.A
-    forms = {
-        "mixed_gs": dict(relaxation=mgldg.RELAX_GAUSS_SEIDEL, omega=0.8, precision=mgldg.PREC_MIXED),
-        "fp64_gs": dict(relaxation=mgldg.RELAX_GAUSS_SEIDEL, omega=0.8, precision=mgldg.PREC_FP64),
-        "mixed_jacobi": dict(relaxation=mgldg.RELAX_JACOBI, omega=0.7, precision=mgldg.PREC_MIXED),
-        "fp64_jacobi": dict(relaxation=mgldg.RELAX_JACOBI, omega=0.7, precision=mgldg.PREC_FP64),
-    }
-    headline = "mixed_gs"
+    names = [f for f in args.forms.split(",") if f]
+    for f in names:
+        if f not in FORMS:
+            raise SystemExit(f"unknown form {f}")
+    headline = args.headline if args.headline in names else names[0]
     hist = np.zeros(WL["maxit"])
 
-    def solve(mg):
+    def solve(mg, xbuf, tol=WL["tol"]):
         with torch.cuda.stream(ext):
-            x.zero_()
+            xbuf.zero_()
         it = C.c_int()
-        ctx.check(L.mgldg_pcg_dev(ctx.h, mg.h, A.h, C.c_void_p(b.data_ptr()), C.c_void_p(x.data_ptr()), WL["tol"],
+        ctx.check(L.mgldg_pcg_dev(ctx.h, mg.h, A.h, C.c_void_p(b.data_ptr()), C.c_void_p(xbuf.data_ptr()), tol,
                                   WL["maxit"], C.byref(it), hist), "pcg")
         return it.value
 
-    def timed(mg, steps, warmup, prof=False):
-        for _ in range(warmup):
-            solve(mg)
+    def timed(mg):
+        # timed region: the solves as a user runs them (V-cycles replayed as
+        # CUDA graphs); then the same steps again with per-kernel CUDA-event
+        # timing on the library's stream (eager launches) for the breakdown
+        for _ in range(args.warmup):
+            solve(mg, x)
         torch.cuda.synchronize()
         ctx.sync()
         dist_barrier(ws)
-        if prof:
-            ctx.prof_reset()
-            ctx.prof_enable(True)
+        ctx.prof_reset()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(ext)
-        iters = [solve(mg) for _ in range(steps)]
+        iters = [solve(mg, x) for _ in range(args.steps)]
         e1.record(ext)
         e1.synchronize()
         ctx.sync()
-        ms = e0.elapsed_time(e1) / steps
-        prof_out = None
-        if prof:
-            prof_out = ctx.prof()
-            ctx.prof_enable(False)
+        ms = e0.elapsed_time(e1) / args.steps
+        launches = ctx.prof()
         torch.cuda.synchronize()
         dist_barrier(ws)
-        return dist_max(ms, ws), iters, prof_out
+        ctx.prof_reset()
+        ctx.prof_enable(True)
+        for _ in range(args.steps):
+            solve(mg, x)
+        prof = ctx.prof()
+        ctx.prof_enable(False)
+        prof = {k: (launches[k][0], prof[k][1]) for k in prof}
+        return dist_max(ms, ws), iters, prof
 
-    results, setup_ms, mgs = {}, {}, {}
-    xref = None
-    for name, kw in forms.items():
+    mgs, setup_ms = {}, {}
+    for name in names:
+        relax, omega, prec = FORMS[name]
         t0 = time.perf_counter()
-        mg = mgldg.Multigrid(ctx, prob.ops, prob.T, npre=WL["npre"], npost=WL["npost"],
-                             solver=mgldg.COARSE_DENSE, max_levels=levels, mean_project=0, **kw)
+        mgs[name] = mgldg.Multigrid(ctx, prob.ops, prob.T, npre=WL["npre"], npost=WL["npost"],
+                                    solver=mgldg.COARSE_DENSE, max_levels=levels, mean_project=0,
+                                    relaxation=relax, omega=omega, precision=prec)
         setup_ms[name] = (time.perf_counter() - t0) * 1e3
-        mgs[name] = mg
+    bh = b.cpu().numpy()
+    results, profs = {}, {}
     clocks = Clocks(local)
     clocks.start()
-    out_prof = None
-    for name in forms:
-        ms, iters, prof = timed(mgs[name], args.steps, args.warmup, prof=(name == headline))
+    for name in names:
+        ms, iters, prof = timed(mgs[name])
         xs = x.cpu().numpy().copy()
-        bh = b.cpu().numpy()
         res = A.mv(xs, alpha=-1.0, beta=1.0, y=bh)
         results[name] = dict(ms=ms, iters=iters[-1], rel_residual=float(np.linalg.norm(res) / np.linalg.norm(bh)),
-                             x=xs)
-        if name == headline:
-            out_prof = prof
+                             kernel_ms={k: round(v[1] / args.steps, 4) for k, v in prof.items() if v[0]},
+                             launches_per_solve=int(sum(v[0] for v in prof.values()) / args.steps), x=xs)
+        profs[name] = prof
     clk = clocks.stop()
-    # FP64 reference solution for the error of each form (FP64 GS to 1e-13)
-    with torch.cuda.stream(ext):
-        x.zero_()
-    it = C.c_int()
-    ctx.check(L.mgldg_pcg_dev(ctx.h, mgs["fp64_gs"].h, A.h, C.c_void_p(b.data_ptr()), C.c_void_p(x.data_ptr()),
-                              1e-13, WL["maxit"], C.byref(it), hist), "pcg ref")
-    ctx.sync()
-    xref = x.cpu().numpy().copy()
-    for name in forms:
+    # FP64 reference solution (FP64 form to 1e-13) for each form's error
+    ref_form = "fp64_gs" if "fp64_gs" in mgs else ("fp64_jacobi" if "fp64_jacobi" in mgs else None)
+    xref = None
+    if ref_form:
+        solve(mgs[ref_form], x, tol=1e-13)
+        ctx.sync()
+        xref = x.cpu().numpy().copy()
+    for name in names:
         xs = results[name].pop("x")
-        results[name]["rel_error_vs_fp64"] = float(np.linalg.norm(xs - xref) / np.linalg.norm(xref))
+        if xref is not None:
+            results[name]["rel_error_vs_fp64"] = float(np.linalg.norm(xs - xref) / np.linalg.norm(xref))
 
     # SpMV bandwidth (FP64, the outer CG operator)
-    s64 = level_bytes(mgs["fp64_gs"], 1, 8)[0]["spmv"]
+    nbr, _, br, _, nnzb = A.info()
+    s64 = nnzb * br * br * 8 + 4 * nnzb + 4 * (nbr + 1) + 2 * ndof * 8
     y = torch.empty_like(x)
     for _ in range(3):
         ctx.check(L.mgldg_bsr_mv_dev(ctx.h, 1.0, A.h, C.c_void_p(b.data_ptr()), 0.0, C.c_void_p(y.data_ptr())), "mv")
@@ -281,64 +321,78 @@ def run_gpu(args, ws, rank, local):
     e1.synchronize()
     spmv_ms = e0.elapsed_time(e1) / nrep
     hbm, peak_kind = peaks()
+    fp64_tf = fp64_peak_tflops(torch)
 
     # roofline of the dominant kernel class of the headline form
-    mgh = mgs[headline]
-    s = 4 if forms[headline]["precision"] == mgldg.PREC_MIXED else 8
-    lb = level_bytes(mgh, levels - 1, s)
-    cls = max(out_prof, key=lambda k: out_prof[k][1])
-    vcycles = sum(1 for _ in range(args.steps)) * (results[headline]["iters"] + 1)
-    key = "gs" if forms[headline]["relaxation"] == mgldg.RELAX_GAUSS_SEIDEL else "jacobi"
-    sweep_bytes = vcycles * (WL["npre"] + WL["npost"]) * sum(l[key] for l in lb)
-    launches, cls_ms = out_prof[cls]
+    relax_h, _, prec_h = FORMS[headline]
+    prof = profs[headline]
+    s = 4 if prec_h == 1 else 8
+    lb = level_bytes(mgs[headline], levels - 1, s)
+    cls = max(prof, key=lambda k: prof[k][1])
+    launches, cls_ms = prof[cls]
+    vcycles = args.steps * (results[headline]["iters"] + 1)
     if cls in ("gauss_seidel", "jacobi"):
-        algo_bytes = sweep_bytes
+        key = "gs" if cls == "gauss_seidel" else "jacobi"
+        algo = vcycles * (WL["npre"] + WL["npost"]) * sum(l[key] for l in lb)
+    elif cls == "spmv":
+        # outer FP64 products (one per iteration plus the initial residual and
+        # the replacements) and the level residuals in the V-cycle
+        outer = args.steps * (results[headline]["iters"] + 1 + (results[headline]["iters"] - 1) // 50 + 1)
+        algo = outer * s64 + vcycles * sum(l["spmv"] for l in lb)
     else:
-        algo_bytes = None
-    achieved = algo_bytes / (cls_ms * 1e-3) / 1e9 if algo_bytes else None
+        algo = None
+    achieved = algo / (cls_ms * 1e-3) / 1e9 if algo else None
     roof = {"bound": "hbm", "kernel": cls, "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": (achieved / hbm) if achieved else None, "traffic": None, "peak_kind": peak_kind,
             "launches": launches, "avg_launch_ms": cls_ms / max(1, launches),
-            "algorithmic_bytes_per_launch": (algo_bytes / launches) if algo_bytes else None}
-    gpu_launches = int(sum(v[0] for v in out_prof.values()))
+            "algorithmic_bytes_per_launch": (algo / launches) if algo else None}
+    gpu_launches = int(sum(v[0] for v in prof.values()))
 
     # end to end through the public host API: pinned host b -> device, solve,
     # x -> host, every step
-    bh = torch.empty(ndof, dtype=torch.float64, pin_memory=True)
-    bh.copy_(b.cpu())
-    xh = torch.zeros(ndof, dtype=torch.float64, pin_memory=True)
-    bnp, xnp = bh.numpy(), xh.numpy()
+    bpin = torch.empty(ndof, dtype=torch.float64, pin_memory=True)
+    bpin.copy_(b.cpu())
+    xpin = torch.zeros(ndof, dtype=torch.float64, pin_memory=True)
+    bnp, xnp = bpin.numpy(), xpin.numpy()
     e2e = []
     for k in range(args.warmup + args.steps):
         xnp[:] = 0.0
         dist_barrier(ws)
         t0 = time.perf_counter()
-        _, hh = mgldg.pcg(ctx, A, bnp, x=xnp, precon=mgs[headline], tol=WL["tol"], maxit=WL["maxit"])
+        mgldg.pcg(ctx, A, bnp, x=xnp, precon=mgs[headline], tol=WL["tol"], maxit=WL["maxit"])
         dt = time.perf_counter() - t0
         if k >= args.warmup:
             e2e.append(dt * 1e3)
     e2e_ms = dist_max(float(np.mean(e2e)), ws)
 
+    speedup = {}
+    for sm in ("gs", "jacobi"):
+        if f"fp64_{sm}" in results and f"mixed_{sm}" in results:
+            speedup[sm] = results[f"fp64_{sm}"]["ms"] / results[f"mixed_{sm}"]["ms"]
+    f64 = [results[f]["ms"] for f in results if f.startswith("fp64")]
+    mx = [results[f]["ms"] for f in results if f.startswith("mixed")]
+    if f64 and mx:
+        speedup["best_mixed_vs_best_fp64"] = min(f64) / min(mx)
+
     line = {
         "metric": METRIC, "value": results[headline]["ms"], "unit": "ms", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": results[headline]["ms"], "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 V-cycle / f64 CG",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 V-cycle / f64 CG" if prec_h == 1 else "f64",
         "data": f"synthetic: seeded 8-Gaussian forcing (seed {WL['seed']}), homogeneous Dirichlet",
-        "config": {"workload": workload_name(n, P, levels), "form": "mixed precision, block Gauss-Seidel omega=0.8",
+        "config": {"workload": workload_name(n, P, levels), "form": FORM_TEXT[headline],
                    "parallelism": "replicas" if ws > 1 else "single GPU",
                    "l2": "inputs larger than L2 (A is 2.68 GB in FP64, 1.34 GB in FP32)"},
         "forms": results,
-        "mixed_vs_fp64_speedup": {"gs": results["fp64_gs"]["ms"] / results["mixed_gs"]["ms"],
-                                  "jacobi": results["fp64_jacobi"]["ms"] / results["mixed_jacobi"]["ms"],
-                                  "best_mixed_vs_best_fp64": min(results["fp64_gs"]["ms"], results["fp64_jacobi"]["ms"]) /
-                                  min(results["mixed_gs"]["ms"], results["mixed_jacobi"]["ms"])},
+        "mixed_vs_fp64_speedup": speedup,
         "spmv": {"precision": "fp64", "ms": spmv_ms, "gbs": s64 / (spmv_ms * 1e-3) / 1e9, "bytes": s64,
-                 "frac_of_hbm": s64 / (spmv_ms * 1e-3) / 1e9 / hbm},
+                 "frac_of_hbm": s64 / (spmv_ms * 1e-3) / 1e9 / hbm,
+                 "fp64_tflops": 2 * nnzb * br * br / (spmv_ms * 1e-3) / 1e12,
+                 "fp64_peak_tflops_cublas": fp64_tf},
         "setup_ms": {"problem_build": t_build * 1e3, **setup_ms},
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 2 * ndof * 8, "d2h_bytes_per_step": ndof * 8,
                 "api": "mgldg_pcg (host buffers, pinned)"},
         "roofline": roof,
-        "kernel_breakdown_ms": {k: v[1] for k, v in out_prof.items()},
         "gpu_launches": gpu_launches,
         "clocks": clk,
     }
@@ -353,14 +407,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=WL["n"])
     ap.add_argument("--levels", type=int, default=WL["levels"])
+    ap.add_argument("--forms", default="mixed_jacobi,fp64_jacobi,mixed_gs,fp64_gs")
+    ap.add_argument("--headline", default="mixed_jacobi")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         if rank == 0:
-            iters = 14
-            cb = cpu_baseline(args.n, WL["P"], args.levels, iters, WL["tol"], WL["seed"])
-            samples = [cb["value"]]
+            cb = cpu_baseline(args.n, WL["P"], args.levels, REF_ITERS, WL["tol"], WL["seed"])
             line = {"metric": METRIC, "value": cb["value"], "unit": "ms", "n_gpus": ws, "steps": 1, "warmup": 0,
                     "ms_per_step": cb["value"], "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
                     "dtype": "f64", "data": f"synthetic: seeded 8-Gaussian forcing (seed {WL['seed']})",
@@ -369,7 +423,6 @@ def main():
                     "impl": "reference",
                     "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
                     "e2e": {"value": cb["value"], "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-            del samples
             print(json.dumps(line), flush=True)
         return
     t0 = time.perf_counter()
@@ -377,10 +430,9 @@ def main():
     print(f"[bench] GPU part {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
     if rank == 0:
         if ws == 1 and not args.no_cpu:
-            line["cpu_baseline"] = {k: v for k, v in cpu_baseline(args.n, WL["P"], args.levels,
-                                                                  results["fp64_gs"]["iters"], WL["tol"],
-                                                                  WL["seed"]).items()
-                                    if k in ("value", "unit", "cores", "kind", "sample")}
+            iters = results["fp64_gs"]["iters"] if "fp64_gs" in results else REF_ITERS
+            cb = cpu_baseline(args.n, WL["P"], args.levels, iters, WL["tol"], WL["seed"])
+            line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
         print(f"[bench] total {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
         print(json.dumps(line), flush=True)
 

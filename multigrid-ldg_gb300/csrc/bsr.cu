@@ -18,6 +18,7 @@
 
 #include "api.cuh"
 #include "master_tables.inc"
+#include "rowdot.cuh"
 
 using namespace mg;
 
@@ -268,14 +269,8 @@ __global__ void __launch_bounds__(WPB * 32)
     const int c0 = s * L::CH;
     double dacc = 0;
     for (int row = blockIdx.x * WPB + warp; row < nbr; row += gridDim.x * WPB) {
-        T acc = 0;
-        const int k0 = row_ptr[row], k1 = row_ptr[row + 1];
-#pragma unroll 2
-        for (int k = k0; k < k1; ++k) {
-            const int j = __ldg(col_idx + k);
-            const T* a = val + (size_t)(blk ? __ldg(blk + k) : k) * (BR * BC);
-            if (active) acc += chunk_dot<T, BR, BC>(a, x + (size_t)j * BC, r, c0);
-        }
+        const int k0 = __ldg(row_ptr + row), k1 = __ldg(row_ptr + row + 1);
+        T acc = row_dot<T, BR, BC, RowDepth<T>::value>(col_idx, val, blk, x, k0, k1, r, c0, active, lane);
         acc = seg_sum<L::S>(acc);
         if (active && s == 0) {
             const size_t o = (size_t)row * BR + r;

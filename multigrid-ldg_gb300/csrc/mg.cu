@@ -76,6 +76,16 @@ struct mgldg_mg {
     int pcg_maxit = 0;
     mg::PcgScalars* sc = nullptr;
     mg::PcgScalars* h_sc = nullptr;   // pinned
+    // preconditioner V-cycles captured as CUDA graphs, keyed by (in, out)
+    struct Graph {
+        const double* in = nullptr;
+        double* out = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        int64_t launches[MGLDG_K_NCLASS] = {0};
+    };
+    Graph graphs[2];
+    int next_graph = 0;
+    bool graphs_off = false;
     ~mgldg_mg();
 };
 
@@ -358,12 +368,70 @@ static void ensure_pcg(mgldg_mg* m, mgldg_ctx* ctx, int64_t n, int maxit) {
     }
 }
 
-static void precon(mgldg_mg* m, const double* r, double* s) {
-    if (m->L.empty()) {
-        MG_CHECK_CUDA(cudaMemcpyAsync(s, r, m->pcg_n * sizeof(double), cudaMemcpyDeviceToDevice, m->ctx->stream));
-    } else {
-        vcycle_dev(m, r, s, true);
+// Captures one preconditioner application (x = 0, b = r, V-cycle, s = x) as
+// a CUDA graph.  Returns null (and stops trying) if the capture is refused.
+static mgldg_mg::Graph* capture_precon(mgldg_mg* m, const double* r, double* s) {
+    mgldg_ctx* ctx = m->ctx;
+    mgldg_mg::Graph& g = m->graphs[m->next_graph];
+    m->next_graph ^= 1;
+    if (g.exec) {
+        cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
     }
+    int64_t before[MGLDG_K_NCLASS];
+    std::memcpy(before, ctx->launches, sizeof before);
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        m->graphs_off = true;
+        return nullptr;
+    }
+    bool ok = true;
+    try {
+        vcycle_dev(m, r, s, true);
+    } catch (...) {
+        ok = false;
+    }
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+    if (e != cudaSuccess || !ok || !graph) ok = false;
+    if (ok && cudaGraphInstantiate(&g.exec, graph, 0) != cudaSuccess) {
+        g.exec = nullptr;
+        ok = false;
+    }
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    for (int k = 0; k < MGLDG_K_NCLASS; ++k) {
+        g.launches[k] = ctx->launches[k] - before[k];
+        ctx->launches[k] = before[k];   // captured, not run
+    }
+    if (!ok) {
+        m->graphs_off = true;
+        return nullptr;
+    }
+    g.in = r;
+    g.out = s;
+    return &g;
+}
+
+static void precon(mgldg_mg* m, const double* r, double* s) {
+    mgldg_ctx* ctx = m->ctx;
+    if (m->L.empty()) {
+        MG_CHECK_CUDA(cudaMemcpyAsync(s, r, m->pcg_n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+        return;
+    }
+    // per-kernel event timing needs eager launches
+    if (!ctx->prof && !m->graphs_off) {
+        mgldg_mg::Graph* g = nullptr;
+        for (auto& c : m->graphs)
+            if (c.exec && c.in == r && c.out == s) g = &c;
+        if (!g) g = capture_precon(m, r, s);
+        if (g) {
+            MG_CHECK_CUDA(cudaGraphLaunch(g->exec, ctx->stream));
+            for (int k = 0; k < MGLDG_K_NCLASS; ++k) ctx->launches[k] += g->launches[k];
+            return;
+        }
+    }
+    vcycle_dev(m, r, s, true);
 }
 
 // pcg on device vectors (krylov.h:22-68)
@@ -449,6 +517,8 @@ static void pcg_dev(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const doubl
 
 mgldg_mg::~mgldg_mg() {
     if (ctx) cudaSetDevice(ctx->device);
+    for (auto& g : graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
     for (auto& L : this->L) {
         if (L.owns_ops) delete L.ops;
         dfree(L.Dinv); dfree(L.Dinv32);

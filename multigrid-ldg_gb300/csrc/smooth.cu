@@ -23,6 +23,7 @@
 #include <algorithm>
 
 #include "api.cuh"
+#include "rowdot.cuh"
 #include "smooth.cuh"
 
 using namespace mg;
@@ -200,24 +201,29 @@ __global__ void __launch_bounds__(WPB * 32)
     const bool active = r < B;
     const int c0 = s * L::CH;
     for (int i = blockIdx.x * WPB + warp; i < n; i += gridDim.x * WPB) {
-        T acc = 0;
-        const int k0 = row_ptr[i], k1 = row_ptr[i + 1];
-#pragma unroll 2
-        for (int k = k0; k < k1; ++k) {
-            const int j = __ldg(col_idx + k);
-            if (active) {
-                const T* a = val + (size_t)k * B * B;
-                const T* xj = xin + (size_t)j * B;
-#pragma unroll
-                for (int c = 0; c < L::CH; ++c)
-                    if (c0 + c < B) acc += __ldg(a + r * B + c0 + c) * __ldg(xj + c0 + c);
-            }
+        // the row's own data is independent of the product: issue it first
+        T bi = 0, xi = 0;
+        if (active && s == 0) {
+            bi = __ldg(b + (size_t)i * B + r);
+            xi = __ldg(xin + (size_t)i * B + r);
         }
+        T dch[L::CH];
+        const T* Di = Dinv + (size_t)i * B * B;
+#pragma unroll
+        for (int c = 0; c < L::CH; ++c) dch[c] = (active && c0 + c < B) ? __ldg(Di + r * B + c0 + c) : T(0);
+        const int k0 = __ldg(row_ptr + i), k1 = __ldg(row_ptr + i + 1);
+        T acc = row_dot<T, B, B, RowDepth<T>::value>(col_idx, val, nullptr, xin, k0, k1, r, c0, active, lane);
         acc = seg_sum<L::S>(acc);
-        T t = 0;
-        if (active && s == 0) t = b[(size_t)i * B + r] - acc;
-        const T y = apply_block<T, B>(Dinv + (size_t)i * B * B, t, r, c0);
-        if (active && s == 0) xout[(size_t)i * B + r] = xin[(size_t)i * B + r] + omega * y;
+        const T t = (active && s == 0) ? bi - acc : T(0);
+        T y = 0;
+#pragma unroll
+        for (int c = 0; c < L::CH; ++c) {
+            const int cc = c0 + c;
+            const T tc = __shfl_sync(0xffffffffu, t, (cc * L::S) & 31);
+            if (cc < B && active) y += dch[c] * tc;
+        }
+        y = seg_sum<L::S>(y);
+        if (active && s == 0) xout[(size_t)i * B + r] = xi + omega * y;
     }
 }
 
