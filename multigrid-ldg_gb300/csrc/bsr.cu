@@ -257,7 +257,7 @@ __device__ __forceinline__ T chunk_dot(const T* __restrict__ a, const T* __restr
 }
 
 template <class T, int BR, int BC, int WPB>
-__global__ void __launch_bounds__(WPB * 32)
+__global__ void __launch_bounds__(WPB * 32, 2)
     k_spmv(int nbr, const int* __restrict__ row_ptr, const int* __restrict__ col_idx,
            const T* __restrict__ val, const int* __restrict__ blk, T alpha, const T* __restrict__ x, T beta,
            const T* yin, T* y, const T* dotv, int self_dot, double* __restrict__ partials) {
@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(WPB * 32)
     double dacc = 0;
     for (int row = blockIdx.x * WPB + warp; row < nbr; row += gridDim.x * WPB) {
         const int k0 = __ldg(row_ptr + row), k1 = __ldg(row_ptr + row + 1);
-        T acc = row_dot<T, BR, BC, RowDepth<T>::value>(col_idx, val, blk, x, k0, k1, r, c0, active, lane);
+        T acc = row_product<T, BR, BC>(col_idx, val, blk, x, k0, k1, r, c0, active, lane);
         acc = seg_sum<L::S>(acc);
         if (active && s == 0) {
             const size_t o = (size_t)row * BR + r;
@@ -324,6 +324,57 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Interpolation-type operators (restriction T^T, prolongation T): a handful
+// of distinct blocks and one to four blocks per row.  One thread per output
+// entry; the block table is staged in shared memory with rows padded to
+// BC+1 values (conflict-free across the BR rows of a block).
+template <class T, int BR, int BC>
+__global__ void __launch_bounds__(256)
+    k_transfer(int nbr, const int* __restrict__ row_ptr, const int* __restrict__ col_idx,
+               const T* __restrict__ table, int ntab, const int* __restrict__ blk, T alpha,
+               const T* __restrict__ x, T beta, const T* yin, T* y) {
+    extern __shared__ unsigned char smraw[];
+    T* st = reinterpret_cast<T*>(smraw);
+    constexpr int LD = BC + 1;
+    for (int q = threadIdx.x; q < ntab * BR * BC; q += 256) {
+        const int b = q / (BR * BC), e = q - b * (BR * BC);
+        const int rr = e / BC, cc = e - rr * BC;
+        st[(b * BR + rr) * LD + cc] = table[q];
+    }
+    __syncthreads();
+    const int64_t n = (int64_t)nbr * BR;
+    for (int64_t t = (int64_t)blockIdx.x * 256 + threadIdx.x; t < n; t += (int64_t)gridDim.x * 256) {
+        const int row = (int)(t / BR), r = (int)(t - (int64_t)row * BR);
+        T acc = 0;
+        const int k0 = __ldg(row_ptr + row), k1 = __ldg(row_ptr + row + 1);
+        for (int k = k0; k < k1; ++k) {
+            const T* a = st + (__ldg(blk + k) * BR + r) * LD;
+            const T* xj = x + (size_t)__ldg(col_idx + k) * BC;
+#pragma unroll
+            for (int c = 0; c < BC; ++c) acc = fma(a[c], __ldg(xj + c), acc);
+        }
+        T v = alpha * acc;
+        if (beta != T(0)) v += beta * yin[t];
+        y[t] = v;
+    }
+}
+
+template <class T, int BR, int BC>
+static bool launch_transfer(mgldg_ctx* ctx, const mgldg_bsr* A, T alpha, const T* x, T beta, const T* yin, T* y,
+                            int kclass) {
+    const size_t smem = (size_t)A->nuniq * BR * (BC + 1) * sizeof(T);
+    if (smem > 48 * 1024) return false;
+    const int64_t n = (int64_t)A->nbr * BR;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, ctx->sm_count * 16));
+    {
+        Launch L(ctx, kclass);
+        k_transfer<T, BR, BC><<<grid, 256, smem, ctx->stream>>>(A->nbr, A->row_ptr, A->col_idx, bsr_vals<T>(A),
+                                                                (int)A->nuniq, A->blk, alpha, x, beta, yin, y);
+    }
+    check_launch();
+    return true;
+}
+
 template <>
 const double* bsr_vals<double>(const mgldg_bsr* A) { return A->val; }
 template <>
@@ -357,6 +408,19 @@ void spmv(mgldg_ctx* ctx, const mgldg_bsr* A, T alpha, const T* x, T beta, const
         return;
     }
     const int br = A->br, bc = A->bc;
+    // operators stored as a small block table (interpolation on quadtrees)
+    if (A->blk && !dotv && !partials && A->nuniq <= 16) {
+#define MG_TRANSFER_CASE(R)                                                                            \
+        if (br == R && bc == R && launch_transfer<T, R, R>(ctx, A, alpha, x, beta, yin, y, kclass)) {  \
+            if (npart) *npart = 0;                                                                     \
+            return;                                                                                    \
+        }
+        MG_TRANSFER_CASE(4)
+        MG_TRANSFER_CASE(9)
+        MG_TRANSFER_CASE(16)
+        MG_TRANSFER_CASE(25)
+#undef MG_TRANSFER_CASE
+    }
 #define MG_SPMV_CASE(R, Cc)                                                                            \
     if (br == R && bc == Cc) {                                                                         \
         launch_spmv<T, R, Cc>(ctx, A, alpha, x, beta, yin, y, dotv, partials, npart, kclass);          \

@@ -2,10 +2,11 @@
 //
 // Lane layout: S = 32 / br lanes per block row, each owning a contiguous
 // chunk of CH columns.  For up to MAXB blocks at a time the warp first issues
-// every load of the row -- the column indices (one lane each, broadcast by
-// shuffle), the block values (128-bit loads where the row is 16-byte
-// aligned) and the x chunks -- and only then does the arithmetic, so a warp
-// keeps MAXB blocks in flight instead of one.
+// every load of the row -- the block values (128-bit loads where the row is
+// 16-byte aligned; their addresses need no index), then the column indices
+// (one lane each, broadcast by shuffle) and the x chunks -- and only then
+// does the arithmetic, one fused multiply-add per product, so a warp keeps
+// MAXB blocks in flight instead of one.
 #pragma once
 
 #include "internal.cuh"
@@ -19,15 +20,16 @@ struct V16<double> { typedef double2 type; static constexpr int n = 2; };
 template <>
 struct V16<float> { typedef float4 type; static constexpr int n = 4; };
 
-template <class T>
-__device__ __forceinline__ T vdot(const typename V16<T>::type& a, const typename V16<T>::type& b);
-template <>
-__device__ __forceinline__ double vdot<double>(const double2& a, const double2& b) {
-    return a.x * b.x + a.y * b.y;
+// acc += a . b as a chain of fused multiply-adds (one FMA per product)
+__device__ __forceinline__ void vfma(double& acc, const double2& a, const double2& b) {
+    acc = fma(a.x, b.x, acc);
+    acc = fma(a.y, b.y, acc);
 }
-template <>
-__device__ __forceinline__ float vdot<float>(const float4& a, const float4& b) {
-    return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+__device__ __forceinline__ void vfma(float& acc, const float4& a, const float4& b) {
+    acc = fmaf(a.x, b.x, acc);
+    acc = fmaf(a.y, b.y, acc);
+    acc = fmaf(a.z, b.z, acc);
+    acc = fmaf(a.w, b.w, acc);
 }
 
 // can this block shape use 128-bit loads for every lane chunk?
@@ -51,62 +53,104 @@ __device__ __forceinline__ T row_dot(const int* __restrict__ col_idx, const T* _
     T acc = 0;
     for (int kb = k0; kb < k1; kb += MAXB) {
         const int nb = min(MAXB, k1 - kb);
-        const int jl = (lane < nb) ? __ldg(col_idx + kb + lane) : 0;
-        const int bl = (lane < nb) ? (blk ? __ldg(blk + kb + lane) : kb + lane) : 0;
+        // block values first: their addresses need no loaded index (unless
+        // the matrix stores a block table), so they go out immediately
         if constexpr (RV::ok) {
             typedef typename V16<T>::type V;
             V av[MAXB][RV::NV], xv[MAXB][RV::NV];
 #pragma unroll
+            for (int q = 0; q < MAXB; ++q)
+                if (q < nb && active) {
+                    const int bq = blk ? __ldg(blk + kb + q) : kb + q;
+                    const V* ap = reinterpret_cast<const V*>(val + (size_t)bq * (BR * BC) + r * BC + c0);
+#pragma unroll
+                    for (int v = 0; v < RV::NV; ++v) av[q][v] = __ldg(ap + v);
+                }
+            const int jl = (lane < nb) ? __ldg(col_idx + kb + lane) : 0;
+#pragma unroll
             for (int q = 0; q < MAXB; ++q) {
                 const int j = __shfl_sync(0xffffffffu, jl, q);
-                const int bq = __shfl_sync(0xffffffffu, bl, q);
                 if (q < nb && active) {
-                    const V* ap = reinterpret_cast<const V*>(val + (size_t)bq * (BR * BC) + r * BC + c0);
                     const V* xp = reinterpret_cast<const V*>(x + (size_t)j * BC + c0);
 #pragma unroll
-                    for (int v = 0; v < RV::NV; ++v) {
-                        av[q][v] = __ldg(ap + v);
-                        xv[q][v] = XL ? __ldg(xp + v) : __ldcg(xp + v);
-                    }
+                    for (int v = 0; v < RV::NV; ++v) xv[q][v] = XL ? __ldg(xp + v) : __ldcg(xp + v);
                 }
             }
 #pragma unroll
             for (int q = 0; q < MAXB; ++q)
                 if (q < nb && active) {
 #pragma unroll
-                    for (int v = 0; v < RV::NV; ++v) acc += vdot<T>(av[q][v], xv[q][v]);
+                    for (int v = 0; v < RV::NV; ++v) vfma(acc, av[q][v], xv[q][v]);
                 }
         } else {
             T av[MAXB][L::CH], xv[MAXB][L::CH];
 #pragma unroll
+            for (int q = 0; q < MAXB; ++q)
+                if (q < nb && active) {
+                    const int bq = blk ? __ldg(blk + kb + q) : kb + q;
+                    const T* ap = val + (size_t)bq * (BR * BC) + r * BC + c0;
+#pragma unroll
+                    for (int c = 0; c < L::CH; ++c) av[q][c] = (c0 + c < BC) ? __ldg(ap + c) : T(0);
+                }
+            const int jl = (lane < nb) ? __ldg(col_idx + kb + lane) : 0;
+#pragma unroll
             for (int q = 0; q < MAXB; ++q) {
                 const int j = __shfl_sync(0xffffffffu, jl, q);
-                const int bq = __shfl_sync(0xffffffffu, bl, q);
                 if (q < nb && active) {
-                    const T* ap = val + (size_t)bq * (BR * BC) + r * BC + c0;
                     const T* xp = x + (size_t)j * BC + c0;
 #pragma unroll
-                    for (int c = 0; c < L::CH; ++c) {
-                        const bool in = c0 + c < BC;
-                        av[q][c] = in ? __ldg(ap + c) : T(0);
-                        xv[q][c] = in ? (XL ? __ldg(xp + c) : __ldcg(xp + c)) : T(0);
-                    }
+                    for (int c = 0; c < L::CH; ++c)
+                        xv[q][c] = (c0 + c < BC) ? (XL ? __ldg(xp + c) : __ldcg(xp + c)) : T(0);
                 }
             }
 #pragma unroll
             for (int q = 0; q < MAXB; ++q)
                 if (q < nb && active) {
 #pragma unroll
-                    for (int c = 0; c < L::CH; ++c) acc += av[q][c] * xv[q][c];
+                    for (int c = 0; c < L::CH; ++c) acc = fma(av[q][c], xv[q][c], acc);
                 }
         }
     }
     return acc;
 }
 
-// blocks kept in flight per warp: more for FP32 (bandwidth-bound), fewer for
-// FP64 (bound by the FP64 pipes, registers are better spent on occupancy)
-template <class T>
-struct RowDepth { static constexpr int value = sizeof(T) == 4 ? 6 : 3; };
+// One block at a time with 128-bit loads: the lean form for FP64, whose
+// block products are bound by GB300's FP64 pipes rather than by HBM, so
+// registers are better spent on occupancy than on loads in flight.
+template <class T, int BR, int BC>
+__device__ __forceinline__ T row_dot_lean(const int* __restrict__ col_idx, const T* __restrict__ val,
+                                          const int* __restrict__ blk, const T* x, int k0, int k1, int r, int c0,
+                                          bool active) {
+    using L = WL<BR, BC>;
+    using RV = RowVec<T, BR, BC>;
+    T acc = 0;
+#pragma unroll 2
+    for (int k = k0; k < k1; ++k) {
+        const int j = __ldg(col_idx + k);
+        const T* a = val + (size_t)(blk ? __ldg(blk + k) : k) * (BR * BC) + r * BC + c0;
+        const T* xj = x + (size_t)j * BC + c0;
+        if (!active) continue;
+        if constexpr (RV::ok) {
+            typedef typename V16<T>::type V;
+#pragma unroll
+            for (int v = 0; v < RV::NV; ++v) vfma(acc, __ldg(reinterpret_cast<const V*>(a) + v), __ldg(reinterpret_cast<const V*>(xj) + v));
+        } else {
+#pragma unroll
+            for (int c = 0; c < L::CH; ++c)
+                if (c0 + c < BC) acc = fma(__ldg(a + c), __ldg(xj + c), acc);
+        }
+    }
+    return acc;
+}
+
+// (A x)_i partial for this lane: prefetching form for FP32 (HBM-bound, five
+// blocks -- a full 5-point block row -- in flight), lean form for FP64
+template <class T, int BR, int BC>
+__device__ __forceinline__ T row_product(const int* __restrict__ col_idx, const T* __restrict__ val,
+                                         const int* __restrict__ blk, const T* x, int k0, int k1, int r, int c0,
+                                         bool active, int lane) {
+    if constexpr (sizeof(T) == 4) return row_dot<T, BR, BC, 5>(col_idx, val, blk, x, k0, k1, r, c0, active, lane);
+    else return row_dot_lean<T, BR, BC>(col_idx, val, blk, x, k0, k1, r, c0, active);
+}
 
 }  // namespace mg

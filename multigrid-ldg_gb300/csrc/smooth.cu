@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(WPB * 32)
 // ------------------------------------------------------------ Jacobi sweep --
 // x_out_i = x_in_i + omega * Dinv_i (b_i - sum_j A_ij x_in_j)
 template <class T, int B, int WPB>
-__global__ void __launch_bounds__(WPB * 32)
+__global__ void __launch_bounds__(WPB * 32, 2)
     k_jacobi(int n, const int* __restrict__ row_ptr, const int* __restrict__ col_idx, const T* __restrict__ val,
              const T* __restrict__ Dinv, const T* __restrict__ b, const T* __restrict__ xin, T* __restrict__ xout,
              T omega) {
@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(WPB * 32)
 #pragma unroll
         for (int c = 0; c < L::CH; ++c) dch[c] = (active && c0 + c < B) ? __ldg(Di + r * B + c0 + c) : T(0);
         const int k0 = __ldg(row_ptr + i), k1 = __ldg(row_ptr + i + 1);
-        T acc = row_dot<T, B, B, RowDepth<T>::value>(col_idx, val, nullptr, xin, k0, k1, r, c0, active, lane);
+        T acc = row_product<T, B, B>(col_idx, val, nullptr, xin, k0, k1, r, c0, active, lane);
         acc = seg_sum<L::S>(acc);
         const T t = (active && s == 0) ? bi - acc : T(0);
         T y = 0;
