@@ -268,8 +268,16 @@ def run_gpu(args, ws, rank, local):
         for _ in range(args.steps):
             solve(mg, x)
         prof = ctx.prof()
+        # per multigrid level (-1: pcg's own products) of the profiled pass
+        per_level = {}
+        for kid, kname in enumerate(mgldg.K_NAMES):
+            for lvl in range(-1, levels):
+                nl, tl = ctx.prof_level(kid, lvl)
+                if nl:
+                    per_level.setdefault(kname, {})[lvl] = (nl, tl)
         ctx.prof_enable(False)
         prof = {k: (launches[k][0], prof[k][1]) for k in prof}
+        prof["_per_level"] = per_level
         return dist_max(ms, ws), iters, prof
 
     mgs, setup_ms = {}, {}
@@ -286,12 +294,13 @@ def run_gpu(args, ws, rank, local):
     clocks.start()
     for name in names:
         ms, iters, prof = timed(mgs[name])
+        per_level = prof.pop("_per_level")
         xs = x.cpu().numpy().copy()
         res = A.mv(xs, alpha=-1.0, beta=1.0, y=bh)
         results[name] = dict(ms=ms, iters=iters[-1], rel_residual=float(np.linalg.norm(res) / np.linalg.norm(bh)),
                              kernel_ms={k: round(v[1] / args.steps, 4) for k, v in prof.items() if v[0]},
                              launches_per_solve=int(sum(v[0] for v in prof.values()) / args.steps), x=xs)
-        profs[name] = prof
+        profs[name] = (prof, per_level)
     clk = clocks.stop()
     # FP64 reference solution (FP64 form to 1e-13) for each form's error
     ref_form = "fp64_gs" if "fp64_gs" in mgs else ("fp64_jacobi" if "fp64_jacobi" in mgs else None)
@@ -324,29 +333,29 @@ def run_gpu(args, ws, rank, local):
     fp64_tf = fp64_peak_tflops(torch)
 
     # roofline of the dominant kernel class of the headline form
+    # The dominant kernel class of the headline form, taken on the finest level
+    # (its launches carry the bytes; coarse-level launches are a few us each
+    # and their event times include launch gaps).  Algorithmic bytes per
+    # launch come from the level's actual matrix; time from CUDA events on the
+    # library's stream in the profiled pass of the same steps.
     relax_h, _, prec_h = FORMS[headline]
-    prof = profs[headline]
+    prof, per_level = profs[headline]
     s = 4 if prec_h == 1 else 8
     lb = level_bytes(mgs[headline], levels - 1, s)
     cls = max(prof, key=lambda k: prof[k][1])
-    launches, cls_ms = prof[cls]
-    vcycles = args.steps * (results[headline]["iters"] + 1)
-    if cls in ("gauss_seidel", "jacobi"):
-        key = "gs" if cls == "gauss_seidel" else "jacobi"
-        algo = vcycles * (WL["npre"] + WL["npost"]) * sum(l[key] for l in lb)
-    elif cls == "spmv":
-        # outer FP64 products (one per iteration plus the initial residual and
-        # the replacements) and the level residuals in the V-cycle
-        outer = args.steps * (results[headline]["iters"] + 1 + (results[headline]["iters"] - 1) // 50 + 1)
-        algo = outer * s64 + vcycles * sum(l["spmv"] for l in lb)
-    else:
-        algo = None
-    achieved = algo / (cls_ms * 1e-3) / 1e9 if algo else None
-    roof = {"bound": "hbm", "kernel": cls, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": (achieved / hbm) if achieved else None, "traffic": None, "peak_kind": peak_kind,
-            "launches": launches, "avg_launch_ms": cls_ms / max(1, launches),
-            "algorithmic_bytes_per_launch": (algo / launches) if algo else None}
+    key = {"gauss_seidel": "gs", "jacobi": "jacobi", "spmv": "spmv"}.get(cls)
+    roof = {"bound": "hbm", "kernel": cls, "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None,
+            "traffic": None, "peak_kind": peak_kind}
+    if key and 0 in per_level.get(cls, {}):
+        n0, ms0 = per_level[cls][0]
+        bytes0 = lb[0][key]
+        achieved = bytes0 * n0 / (ms0 * 1e-3) / 1e9
+        roof.update(achieved=achieved, frac=achieved / hbm, level=0, launches=n0, avg_launch_ms=ms0 / n0,
+                    algorithmic_bytes_per_launch=bytes0,
+                    all_levels={"launches": prof[cls][0], "ms": prof[cls][1]})
     gpu_launches = int(sum(v[0] for v in prof.values()))
+    results[headline]["per_level_ms"] = {k: {str(l): round(v[1] / args.steps, 4) for l, v in d.items()}
+                                         for k, d in per_level.items()}
 
     # end to end through the public host API: pinned host b -> device, solve,
     # x -> host, every step

@@ -229,6 +229,9 @@ int mgldg_prof_reset(mgldg_ctx* ctx);
 /* Launch count and summed event time (ms) of one kernel class since reset
  * (time only while enabled).  Synchronises the stream. */
 int mgldg_prof_query(mgldg_ctx* ctx, int kclass, int64_t* launches, double* ms);
+/* The same for the launches that worked on one multigrid level (0 = finest;
+ * -1 = work outside the V-cycle, such as pcg's own products). */
+int mgldg_prof_query_level(mgldg_ctx* ctx, int kclass, int level, int64_t* launches, double* ms);
 
 #ifdef __cplusplus
 }

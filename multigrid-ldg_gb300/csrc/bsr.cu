@@ -12,6 +12,7 @@
 // y = alpha*A*x + beta*yin and the partial dot product y.v per CTA (summed in
 // a fixed order afterwards, so results are run-to-run reproducible).
 #include <algorithm>
+#include <type_traits>
 #include <map>
 #include <numeric>
 #include <unordered_map>
@@ -25,8 +26,11 @@ using namespace mg;
 // ================================================================ context ==
 namespace mg {
 
-Launch::Launch(mgldg_ctx* c, int kclass) : ctx(c), kc(kclass) {
+static int prof_slot(int level) { return level < 0 ? 0 : (level + 1 < kProfLevels ? level + 1 : kProfLevels - 1); }
+
+Launch::Launch(mgldg_ctx* c, int kclass) : ctx(c), kc(kclass), lv(prof_slot(c->cur_level)) {
     ctx->launches[kc]++;
+    ctx->lv_launches[kc][lv]++;
     if (ctx->prof) {
         if (ctx->event_pool.size() < 2) {
             for (int i = 0; i < 64; ++i) {
@@ -43,7 +47,7 @@ Launch::Launch(mgldg_ctx* c, int kclass) : ctx(c), kc(kclass) {
 Launch::~Launch() {
     if (a) {
         cudaEventRecord(b, ctx->stream);
-        ctx->pending.push_back(ProfEvent{a, b, kc});
+        ctx->pending.push_back(ProfEvent{a, b, kc, lv});
         if (ctx->pending.size() > 4096) {
             try { prof_flush(ctx); } catch (...) {}
         }
@@ -54,7 +58,10 @@ void prof_flush(mgldg_ctx* ctx) {
     MG_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
     for (auto& p : ctx->pending) {
         float t = 0;
-        if (cudaEventElapsedTime(&t, p.a, p.b) == cudaSuccess) ctx->ms[p.kclass] += t;
+        if (cudaEventElapsedTime(&t, p.a, p.b) == cudaSuccess) {
+            ctx->ms[p.kclass] += t;
+            ctx->lv_ms[p.kclass][p.level] += t;
+        }
         ctx->event_pool.push_back(p.a);
         ctx->event_pool.push_back(p.b);
     }
@@ -81,7 +88,11 @@ extern "C" int mgldg_ctx_create(int device, mgldg_ctx** out) {
         return MGLDG_ERR_CUDA;
     }
     ctx->n_partials = 8192;
-    if (cudaMalloc(&ctx->d_partials, ctx->n_partials * sizeof(double)) != cudaSuccess) {
+    if (cudaMalloc(&ctx->d_partials, ctx->n_partials * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&ctx->d_err, sizeof(unsigned)) != cudaSuccess ||
+        cudaMemset(ctx->d_err, 0, sizeof(unsigned)) != cudaSuccess) {
+        cudaFree(ctx->d_partials);
+        cudaFree(ctx->d_err);
         cudaStreamDestroy(ctx->stream);
         delete ctx;
         return MGLDG_ERR_NOMEM;
@@ -97,6 +108,7 @@ extern "C" int mgldg_ctx_destroy(mgldg_ctx* ctx) {
     for (auto& p : ctx->pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     for (auto e : ctx->event_pool) cudaEventDestroy(e);
     cudaFree(ctx->d_partials);
+    cudaFree(ctx->d_err);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return MGLDG_OK;
@@ -140,7 +152,24 @@ extern "C" int mgldg_prof_enable(mgldg_ctx* ctx, int on) {
 extern "C" int mgldg_prof_reset(mgldg_ctx* ctx) {
     MG_API_BEGIN(ctx)
     prof_flush(ctx);
-    for (int k = 0; k < MGLDG_K_NCLASS; ++k) { ctx->launches[k] = 0; ctx->ms[k] = 0; }
+    for (int k = 0; k < MGLDG_K_NCLASS; ++k) {
+        ctx->launches[k] = 0;
+        ctx->ms[k] = 0;
+        for (int l = 0; l < kProfLevels; ++l) {
+            ctx->lv_launches[k][l] = 0;
+            ctx->lv_ms[k][l] = 0;
+        }
+    }
+    MG_API_END
+}
+
+extern "C" int mgldg_prof_query_level(mgldg_ctx* ctx, int kclass, int level, int64_t* launches, double* ms) {
+    MG_API_BEGIN(ctx)
+    MG_REQUIRE(kclass >= 0 && kclass < MGLDG_K_NCLASS && level >= -1 && level + 1 < kProfLevels, MGLDG_ERR_ARG,
+               "bad kernel class or level");
+    prof_flush(ctx);
+    if (launches) *launches = ctx->lv_launches[kclass][level + 1];
+    if (ms) *ms = ctx->lv_ms[kclass][level + 1];
     MG_API_END
 }
 extern "C" int mgldg_prof_query(mgldg_ctx* ctx, int kclass, int64_t* launches, double* ms) {
@@ -408,6 +437,13 @@ void spmv(mgldg_ctx* ctx, const mgldg_bsr* A, T alpha, const T* x, T beta, const
         return;
     }
     const int br = A->br, bc = A->bc;
+    // FP32 16x16 products without a dot epilogue: bulk-copy pipeline
+    if constexpr (std::is_same<T, float>::value) {
+        if (!dotv && !partials && bulk_spmv_f32(ctx, A, alpha, x, beta, yin, y, kclass)) {
+            if (npart) *npart = 0;
+            return;
+        }
+    }
     // operators stored as a small block table (interpolation on quadtrees)
     if (A->blk && !dotv && !partials && A->nuniq <= 16) {
 #define MG_TRANSFER_CASE(R)                                                                            \
@@ -460,7 +496,8 @@ mgldg_bsr* bsr_new(mgldg_ctx* ctx, int nbr, int nbc, int br, int bc, const std::
     A->nnzb = (int64_t)col_idx.size();
     try {
         A->row_ptr = dalloc<int>(nbr + 1);
-        A->col_idx = dalloc<int>(std::max<size_t>(1, col_idx.size()));
+        // four spare entries: bulk copies of index runs move whole 16-byte words
+        A->col_idx = dalloc<int>(col_idx.size() + 4);
         A->val = dalloc<double>(std::max<size_t>(1, col_idx.size() * A->bsz()));
         upload(ctx, A->row_ptr, row_ptr.data(), row_ptr.size());
         upload(ctx, A->col_idx, col_idx.data(), col_idx.size());
@@ -547,7 +584,7 @@ mgldg_bsr* bsr_transpose(mgldg_ctx* ctx, const mgldg_bsr* A) {
         for (int64_t p = 0; p < A->nnzb; ++p) B->h_blk[p] = A->h_blk[src[p]];
         try {
             B->row_ptr = dalloc<int>(B->nbr + 1);
-            B->col_idx = dalloc<int>(std::max<int64_t>(1, B->nnzb));
+            B->col_idx = dalloc<int>(B->nnzb + 4);
             B->blk = dalloc<int>(std::max<int64_t>(1, B->nnzb));
             B->val = dalloc<double>(std::max<int64_t>(1, A->nuniq * (int64_t)A->bsz()));
             upload(ctx, B->row_ptr, rp.data(), rp.size());

@@ -37,7 +37,9 @@ struct Error : std::runtime_error {
 struct ProfEvent {
     cudaEvent_t a, b;
     int kclass;
+    int level;
 };
+constexpr int kProfLevels = 33;   // multigrid level + 1 (slot 0: work outside a level)
 
 }  // namespace mg
 
@@ -49,11 +51,16 @@ struct mgldg_ctx {
     bool prof = false;
     int64_t launches[MGLDG_K_NCLASS] = {0};
     double ms[MGLDG_K_NCLASS] = {0};
+    int cur_level = -1;   // multigrid level the next launches work on (-1: none)
+    int64_t lv_launches[MGLDG_K_NCLASS][mg::kProfLevels] = {};
+    double lv_ms[MGLDG_K_NCLASS][mg::kProfLevels] = {};
     std::vector<mg::ProfEvent> pending;
     std::vector<cudaEvent_t> event_pool;
     // scratch for deterministic two-stage reductions
     double* d_partials = nullptr;
     int n_partials = 0;
+    // device error word of the bulk-copy kernels (bounded barrier waits)
+    unsigned* d_err = nullptr;
 };
 
 namespace mg {
@@ -63,6 +70,7 @@ namespace mg {
 struct Launch {
     mgldg_ctx* ctx;
     int kc;
+    int lv;
     cudaEvent_t a = nullptr, b = nullptr;
     Launch(mgldg_ctx* c, int kclass);
     ~Launch();
@@ -164,10 +172,14 @@ mgldg_ops* galerkin_rat(mgldg_ctx* ctx, const mgldg_ops* f, const mgldg_bsr* T);
 // dense inverse of an SPD matrix assembled from A (Cholesky), device result
 void dense_spd_inverse(mgldg_ctx* ctx, const mgldg_bsr* A, double* out_inv);
 
-// sum_blocks: out[o] = sum_{t in [tptr[o],tptr[o+1])} table[tidx[t]]
-void sum_blocks(mgldg_ctx* ctx, int nout, int bsz, double* const* outp_dev_unused,
-                const int64_t* out_off, const int* tptr, const int* tidx, const double* table,
-                double* out_base);
+// bulk.cu: FP32 block-row kernels that stream values through shared memory
+// with bulk copies; return false when the shape is not handled
+bool bulk_spmv_f32(mgldg_ctx* ctx, const mgldg_bsr* A, float alpha, const float* x, float beta, const float* yin,
+                   float* y, int kclass);
+bool bulk_jacobi_f32(mgldg_ctx* ctx, const mgldg_bsr* A, const float* vals, const float* Dinv, const float* b,
+                     const float* xin, float* xout, float omega);
+// reads and clears the device error word; throws MGLDG_ERR_TIMEOUT if set
+void take_device_error(mgldg_ctx* ctx);
 
 }  // namespace mg
 

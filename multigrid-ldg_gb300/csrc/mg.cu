@@ -170,6 +170,7 @@ __global__ void k_mean_project(int n, T* b) {
 template <class T>
 static void relax(mgldg_mg* m, int i, int n, bool reverse) {
     LevelData& L = m->L[i];
+    m->ctx->cur_level = i;
     const T* vals = bsr_vals<T>(L.A);
     for (int k = 0; k < n; ++k) {
         if (m->p.relaxation == MGLDG_RELAX_JACOBI) {
@@ -185,6 +186,7 @@ template <class T>
 static void coarse_solve(mgldg_mg* m, int i) {
     LevelData& L = m->L[i];
     mgldg_ctx* ctx = m->ctx;
+    ctx->cur_level = i;
     if (m->p.solver == MGLDG_COARSE_RELAXATION) {
         if (m->p.mean_project) {
             Launch K(ctx, MGLDG_K_COARSE);
@@ -214,12 +216,14 @@ static void vcycle(mgldg_mg* m, int i) {
     LevelData& C = m->L[i + 1];
     relax<T>(m, i, m->p.npre, false);
     // r = b - A x ; b_c = T^T r ; x_c = 0
+    ctx->cur_level = i;
     spmv<T>(ctx, L.A, T(-1), LV<T>::x(L), T(1), LV<T>::b(L), LV<T>::r(L));
     spmv<T>(ctx, L.Tt, T(1), LV<T>::r(L), T(0), (const T*)nullptr, LV<T>::b(C), nullptr, nullptr, nullptr,
             MGLDG_K_TRANSFER);
     MG_CHECK_CUDA(cudaMemsetAsync(LV<T>::x(C), 0, C.n * sizeof(T), ctx->stream));
     vcycle<T>(m, i + 1);
     // x += T x_c
+    ctx->cur_level = i;
     spmv<T>(ctx, L.T, T(1), LV<T>::x(C), T(1), LV<T>::x(L), LV<T>::x(L), nullptr, nullptr, nullptr, MGLDG_K_TRANSFER);
     relax<T>(m, i, m->p.npost, true);
 }
@@ -229,12 +233,17 @@ static void take_errors(mgldg_mg* m) {
     for (auto& L : m->L)
         if (L.has_sched) e |= gs_take_error(m->ctx, L.sched);
     if (e) throw Error(MGLDG_ERR_TIMEOUT, "a Gauss-Seidel dependency wait ran out");
+    take_device_error(m->ctx);
 }
 
 // one V-cycle on device vectors b (FP64) and x (FP64, in/out)
 static void vcycle_dev(mgldg_mg* m, const double* b, double* x, bool x_is_zero) {
     mgldg_ctx* ctx = m->ctx;
     LevelData& L = m->L[0];
+    struct LevelReset {
+        mgldg_ctx* c;
+        ~LevelReset() { c->cur_level = -1; }
+    } reset{ctx};
     if (m->p.precision == MGLDG_PREC_MIXED) {
         convert<double, float>(ctx, L.n, b, L.b32);
         if (x_is_zero) MG_CHECK_CUDA(cudaMemsetAsync(L.x32, 0, L.n * sizeof(float), ctx->stream));

@@ -21,6 +21,7 @@
 // The sweep counter lives in device memory and is advanced by the last CTA
 // to finish, so consecutive sweeps need no host involvement.
 #include <algorithm>
+#include <type_traits>
 
 #include "api.cuh"
 #include "rowdot.cuh"
@@ -391,6 +392,9 @@ template <class T>
 void jacobi_sweep(mgldg_ctx* ctx, const mgldg_bsr* A, const T* vals, const T* Dinv, const T* b, const T* xin,
                   T* xout, T omega) {
     if (A->nbr == 0) return;
+    if constexpr (std::is_same<T, float>::value) {
+        if (bulk_jacobi_f32(ctx, A, vals, Dinv, b, xin, xout, omega)) return;
+    }
     switch (A->br) {
         case 1: launch_jacobi<T, 1>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
         case 4: launch_jacobi<T, 4>(ctx, A, vals, Dinv, b, xin, xout, omega); return;

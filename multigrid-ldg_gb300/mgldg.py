@@ -35,6 +35,7 @@ EXPORTS = [
     "mgldg_problem_destroy", "mgldg_problem_info", "mgldg_problem_ops", "mgldg_problem_interp",
     "mgldg_problem_rhs_gaussian", "mgldg_problem_rhs_gaussian_dev", "mgldg_prof_enable", "mgldg_prof_reset",
     "mgldg_prof_query", "mgldg_gs_levels", "mgldg_selftest_wait_timeout", "mgldg_cg_noalloc_dev",
+    "mgldg_prof_query_level",
 ]
 
 
@@ -126,6 +127,7 @@ def lib():
         L.mgldg_gs_levels.argtypes = [C.c_int, _ip, _ip, C.c_int, _ip, _ip, ip]
         L.mgldg_selftest_wait_timeout.argtypes = [vp, C.c_int64, ip]
         L.mgldg_cg_noalloc_dev.argtypes = [vp, vp, vp, vp, C.c_double, C.c_int, ip, _dp]
+        L.mgldg_prof_query_level.argtypes = [vp, C.c_int, C.c_int, i64p, C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -175,6 +177,12 @@ class Context:
             self.check(lib().mgldg_prof_query(self.h, k, C.byref(n), C.byref(ms)), "prof_query")
             out[name] = (n.value, ms.value)
         return out
+
+    def prof_level(self, kclass, level):
+        """(launches, ms) of one kernel class on one multigrid level (-1: outside the V-cycle)."""
+        n, ms = C.c_int64(), C.c_double()
+        self.check(lib().mgldg_prof_query_level(self.h, kclass, level, C.byref(n), C.byref(ms)), "prof_query_level")
+        return n.value, ms.value
 
     def close(self):
         if getattr(self, "h", None):
