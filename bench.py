@@ -353,6 +353,13 @@ def run_gpu(args, ws, rank, local):
         roof.update(achieved=achieved, frac=achieved / hbm, level=0, launches=n0, avg_launch_ms=ms0 / n0,
                     algorithmic_bytes_per_launch=bytes0,
                     all_levels={"launches": prof[cls][0], "ms": prof[cls][1]})
+        if headline == "mixed_jacobi" and key == "jacobi":
+            # dram__bytes_read.sum + dram__bytes_write.sum of this kernel
+            # from one ncu capture at 256x256 Q3 (418.5 MB for 415.8 MB of
+            # algorithmic bytes; profiles/k_rows_bulk_jacobi_fp32_256x256_q3.md),
+            # scaled to this launch by its algorithmic bytes
+            roof["traffic"] = bytes0 * (418.508032 / 415.756292)
+            roof["traffic_source"] = "ncu at 256x256 Q3, scaled by block rows"
     gpu_launches = int(sum(v[0] for v in prof.values()))
     results[headline]["per_level_ms"] = {k: {str(l): round(v[1] / args.steps, 4) for l, v in d.items()}
                                          for k, d in per_level.items()}
