@@ -197,7 +197,31 @@ int mgldg_problem_interp(mgldg_problem* pr, int l, const mgldg_bsr** T);
  * `seed` (centres U[0,1]^2, widths U[0.05,0.2], amplitudes N(0,1)).
  * _dev writes a device vector. */
 int mgldg_problem_rhs_gaussian(mgldg_ctx* ctx, mgldg_problem* pr, uint64_t seed, double* b);
+/* Transfers for h-, p- and hp-multigrid on uniform meshes; the caller owns
+ * the handle (mgldg_mg_create copies it).  h: one level of
+ * InterpolationHierarchy<2,P> from the (n_fine/2)^2 to the n_fine^2 mesh
+ * (interpolationhierarchy.h:30-82).  p: InterpolationHierarchy<2,Pf,Pc> on
+ * ne elements, the block-diagonal evaluation of the degree-Pc basis at the
+ * Pf nodes (interpolationhierarchy.h:99-129).  Passing a chain
+ * [p transfers..., h levels at the last degree...] to mgldg_mg_create gives
+ * the reference's Multigrid<N,P1,P2,...> (multigrid.h:436-560). */
+int mgldg_cartesian_h_interp(mgldg_ctx* ctx, int n_fine, int P, mgldg_bsr** T);
+int mgldg_cartesian_p_interp(mgldg_ctx* ctx, int ne, int P_fine, int P_coarse, mgldg_bsr** T);
 int mgldg_problem_rhs_gaussian_dev(mgldg_ctx* ctx, mgldg_problem* pr, uint64_t seed, double* b);
+
+/* ---------------------------------------------------------- file formats -- */
+/* Matrix Market dump of a BSR matrix, the format of the reference's
+ * SparseBlockMatrix::write (sparseblockmatrix.tpp:145-164): coordinate real
+ * general, 1-based, every entry of every stored block, 17 significant
+ * digits (blocks in sorted order). */
+int mgldg_bsr_write_mtx(mgldg_ctx* ctx, const mgldg_bsr* A, const char* path);
+/* Reads such a file (e.g. the reference's data/A.mtx) into a BSR matrix with
+ * br x bc blocks; entries of one block position are summed. */
+int mgldg_bsr_read_mtx(mgldg_ctx* ctx, const char* path, int br, int bc, mgldg_bsr** A);
+/* Nodal dump of a host vector u on a Cartesian problem, the reference's
+ * Function::write format (function.h:173-190): "P N ne", then per element
+ * one "x y value" line per node and an empty line. */
+int mgldg_problem_write_fun(mgldg_ctx* ctx, const mgldg_problem* pr, const double* u, const char* path);
 
 /* ------------------------------------------------------------ host logic -- */
 /* Level sets of the block Gauss-Seidel sweep (host only, no GPU needed): for

@@ -270,6 +270,83 @@ static mgldg_bsr* realize(mgldg_ctx* ctx, const Assembly& As, int ne, int b, con
     return A;
 }
 
+// A block-CSR operator with one block per row, given column per row and a
+// table of distinct blocks (br x bc) indexed per row.
+static mgldg_bsr* table_operator(mgldg_ctx* ctx, int nbr, int nbc, int br, int bc, const std::vector<int>& col,
+                                 const std::vector<int>& blk, const std::vector<double>& table) {
+    mgldg_bsr* T = new mgldg_bsr();
+    try {
+        std::vector<int> rp(nbr + 1);
+        for (int k = 0; k <= nbr; ++k) rp[k] = k;
+        T->ctx = ctx;
+        T->nbr = nbr; T->nbc = nbc; T->br = br; T->bc = bc;
+        T->nnzb = nbr;
+        T->nuniq = (int64_t)(table.size() / ((size_t)br * bc));
+        T->h_row_ptr = rp;
+        T->h_col_idx = col;
+        T->h_blk = blk;
+        T->row_ptr = dalloc<int>(nbr + 1);
+        T->col_idx = dalloc<int>(nbr + 4);
+        T->blk = dalloc<int>(std::max(1, nbr));
+        T->val = dalloc<double>(table.size());
+        upload(ctx, T->row_ptr, rp.data(), rp.size());
+        upload(ctx, T->col_idx, col.data(), col.size());
+        upload(ctx, T->blk, blk.data(), blk.size());
+        upload(ctx, T->val, table.data(), table.size());
+    } catch (...) {
+        delete T;
+        throw;
+    }
+    return T;
+}
+
+// h-interpolation from the (nf/2)^2 to the nf^2 uniform mesh at degree P
+// (interpolationhierarchy.h:53-79): fine element k of the Morton order lies
+// in parent k>>2 at child position k&3 = (x bit, y bit); its block evaluates
+// the parent's Lagrange basis at the child's nodes.  Four distinct blocks.
+static mgldg_bsr* h_interp(mgldg_ctx* ctx, int nf, int P) {
+    MG_REQUIRE(P >= 1 && P <= MGLDG_PMAX && nf >= 2 && (nf & (nf - 1)) == 0, MGLDG_ERR_ARG,
+               "h-interpolation needs P in 1..6 and a power-of-two n >= 2");
+    const Ref2 R(P);
+    const int b = R.b;
+    std::vector<double> E4((size_t)4 * b * b);
+    for (int cpos = 0; cpos < 4; ++cpos) {
+        const double lo[2] = {0.5 * (cpos >> 1), 0.5 * (cpos & 1)};
+        for (int i0 = 0; i0 < P; ++i0)
+            for (int i1 = 0; i1 < P; ++i1) {
+                double node[2];
+                int idx[2] = {i0, i1};
+                for (int d = 0; d < 2; ++d) node[d] = lo[d] + 0.5 * R.nodes[idx[d]];
+                R.lagrange2(node, &E4[(size_t)cpos * b * b + (size_t)(i0 * P + i1) * b]);
+            }
+    }
+    const int nef = nf * nf;
+    std::vector<int> col(nef), blk(nef);
+    for (int k = 0; k < nef; ++k) {
+        col[k] = k >> 2;
+        blk[k] = k & 3;
+    }
+    return table_operator(ctx, nef, nef / 4, b, b, col, blk, E4);
+}
+
+// p-interpolation from degree Pc to degree Pf on the same ne elements
+// (interpolationhierarchy.h:109-129): every block evaluates the Pc Lagrange
+// basis at the Pf nodes of the master element.  One distinct block.
+static mgldg_bsr* p_interp(mgldg_ctx* ctx, int ne, int Pf, int Pc) {
+    MG_REQUIRE(Pf >= 1 && Pf <= MGLDG_PMAX && Pc >= 1 && Pc <= MGLDG_PMAX && ne >= 1, MGLDG_ERR_ARG,
+               "p-interpolation needs degrees in 1..6 and at least one element");
+    const Ref2 Rf(Pf), Rc(Pc);
+    std::vector<double> E((size_t)Rf.b * Rc.b);
+    for (int i0 = 0; i0 < Pf; ++i0)
+        for (int i1 = 0; i1 < Pf; ++i1) {
+            const double node[2] = {Rf.nodes[i0], Rf.nodes[i1]};
+            Rc.lagrange2(node, &E[(size_t)(i0 * Pf + i1) * Rc.b]);
+        }
+    std::vector<int> col(ne), blk(ne, 0);
+    for (int k = 0; k < ne; ++k) col[k] = k;
+    return table_operator(ctx, ne, ne, Rf.b, Rc.b, col, blk, E);
+}
+
 static mgldg_problem* cartesian_create(mgldg_ctx* ctx, int P, int n, double tau0, double tauD) {
     MG_REQUIRE(P >= 1 && P <= 5, MGLDG_ERR_UNSUPPORTED, "P must be 1..5 (block size <= 25)");
     MG_REQUIRE(n >= 1 && n <= 32768 && (n & (n - 1)) == 0, MGLDG_ERR_ARG, "n must be a power of two");
@@ -431,47 +508,7 @@ static mgldg_problem* cartesian_create(mgldg_ctx* ctx, int P, int n, double tau0
         upload(ctx, pr->d_M, Mblk.data(), Mblk.size());
 
         // ---- h-interpolation hierarchy (interpolationhierarchy.h:30-82) ----
-        // fine element k of level l lies in parent k>>2 at child position
-        // k&3 = (x bit, y bit); its block evaluates the parent's Lagrange
-        // basis at the child's nodes.  Four distinct blocks per level.
-        std::vector<double> E4((size_t)4 * b * b);
-        for (int cpos = 0; cpos < 4; ++cpos) {
-            const double lo[2] = {0.5 * (cpos >> 1), 0.5 * (cpos & 1)};
-            for (int i0 = 0; i0 < P; ++i0)
-                for (int i1 = 0; i1 < P; ++i1) {
-                    double node[2];
-                    int idx[2] = {i0, i1};
-                    for (int d = 0; d < 2; ++d) node[d] = lo[d] + 0.5 * R.nodes[idx[d]];
-                    R.lagrange2(node, &E4[(size_t)cpos * b * b + (size_t)(i0 * P + i1) * b]);
-                }
-        }
-        for (int nf = n; nf > 1; nf >>= 1) {
-            const int nef = nf * nf, nec = nef / 4;
-            std::vector<int> rp(nef + 1), ci(nef);
-            mgldg_bsr* Tl = new mgldg_bsr();
-            pr->T.push_back(Tl);
-            Tl->ctx = ctx;
-            Tl->nbr = nef; Tl->nbc = nec; Tl->br = b; Tl->bc = b;
-            Tl->nnzb = nef; Tl->nuniq = 4;
-            Tl->h_blk.resize(nef);
-            for (int k = 0; k < nef; ++k) {
-                rp[k] = k;
-                ci[k] = k >> 2;
-                Tl->h_blk[k] = k & 3;
-            }
-            rp[nef] = nef;
-            Tl->h_row_ptr = rp;
-            Tl->h_col_idx = ci;
-            Tl->row_ptr = dalloc<int>(nef + 1);
-            Tl->col_idx = dalloc<int>(nef);
-            Tl->blk = dalloc<int>(nef);
-            Tl->val = dalloc<double>(E4.size());
-            upload(ctx, Tl->row_ptr, rp.data(), rp.size());
-            upload(ctx, Tl->col_idx, ci.data(), ci.size());
-            upload(ctx, Tl->blk, Tl->h_blk.data(), nef);
-            upload(ctx, Tl->val, E4.data(), E4.size());
-            (void)nec;
-        }
+        for (int nf = n; nf > 1; nf >>= 1) pr->T.push_back(h_interp(ctx, nf, P));
         sync(ctx);
     } catch (...) {
         dfree(d_table);
@@ -517,6 +554,13 @@ extern "C" int mgldg_problem_destroy(mgldg_problem* pr) {
     return MGLDG_OK;
 }
 
+namespace mg {
+void problem_geometry(const mgldg_problem* pr, int* P, int* n) {
+    *P = pr->P;
+    *n = pr->n;
+}
+}  // namespace mg
+
 extern "C" int mgldg_problem_info(const mgldg_problem* pr, int* ne, int* npl, int64_t* ndof, int* nT) {
     if (!pr) return MGLDG_ERR_ARG;
     if (ne) *ne = pr->ne;
@@ -559,5 +603,23 @@ extern "C" int mgldg_problem_rhs_gaussian(mgldg_ctx* ctx, mgldg_problem* pr, uin
         throw;
     }
     dfree(d);
+    MG_API_END
+}
+
+extern "C" int mgldg_cartesian_h_interp(mgldg_ctx* ctx, int n_fine, int P, mgldg_bsr** T) {
+    MG_API_BEGIN(ctx)
+    MG_REQUIRE(T != nullptr, MGLDG_ERR_ARG, "null output");
+    *T = nullptr;
+    *T = h_interp(ctx, n_fine, P);
+    sync(ctx);
+    MG_API_END
+}
+
+extern "C" int mgldg_cartesian_p_interp(mgldg_ctx* ctx, int ne, int P_fine, int P_coarse, mgldg_bsr** T) {
+    MG_API_BEGIN(ctx)
+    MG_REQUIRE(T != nullptr, MGLDG_ERR_ARG, "null output");
+    *T = nullptr;
+    *T = p_interp(ctx, ne, P_fine, P_coarse);
+    sync(ctx);
     MG_API_END
 }

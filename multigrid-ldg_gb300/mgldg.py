@@ -35,7 +35,8 @@ EXPORTS = [
     "mgldg_problem_destroy", "mgldg_problem_info", "mgldg_problem_ops", "mgldg_problem_interp",
     "mgldg_problem_rhs_gaussian", "mgldg_problem_rhs_gaussian_dev", "mgldg_prof_enable", "mgldg_prof_reset",
     "mgldg_prof_query", "mgldg_gs_levels", "mgldg_selftest_wait_timeout", "mgldg_cg_noalloc_dev",
-    "mgldg_prof_query_level",
+    "mgldg_prof_query_level", "mgldg_cartesian_h_interp", "mgldg_cartesian_p_interp",
+    "mgldg_bsr_write_mtx", "mgldg_bsr_read_mtx", "mgldg_problem_write_fun",
 ]
 
 
@@ -128,6 +129,11 @@ def lib():
         L.mgldg_selftest_wait_timeout.argtypes = [vp, C.c_int64, ip]
         L.mgldg_cg_noalloc_dev.argtypes = [vp, vp, vp, vp, C.c_double, C.c_int, ip, _dp]
         L.mgldg_prof_query_level.argtypes = [vp, C.c_int, C.c_int, i64p, C.POINTER(C.c_double)]
+        L.mgldg_cartesian_h_interp.argtypes = [vp, C.c_int, C.c_int, pvp]
+        L.mgldg_cartesian_p_interp.argtypes = [vp, C.c_int, C.c_int, C.c_int, pvp]
+        L.mgldg_bsr_write_mtx.argtypes = [vp, vp, C.c_char_p]
+        L.mgldg_bsr_read_mtx.argtypes = [vp, C.c_char_p, C.c_int, C.c_int, pvp]
+        L.mgldg_problem_write_fun.argtypes = [vp, vp, _dp, C.c_char_p]
         _lib = L
     return _lib
 
@@ -240,6 +246,16 @@ class SparseBlockMatrix:
         y = np.zeros(nbc * bc)
         self.ctx.check(lib().mgldg_bsr_mv_t(self.ctx.h, self.h, np.ascontiguousarray(x, np.float64), y), "bsr_mv_t")
         return y
+
+    def write_mtx(self, path):
+        """Matrix Market dump (the reference's SparseBlockMatrix::write format)."""
+        self.ctx.check(lib().mgldg_bsr_write_mtx(self.ctx.h, self.h, str(path).encode()), "write_mtx")
+
+    @classmethod
+    def read_mtx(cls, ctx, path, br, bc):
+        h = C.c_void_p()
+        ctx.check(lib().mgldg_bsr_read_mtx(ctx.h, str(path).encode(), br, bc, C.byref(h)), "read_mtx")
+        return cls(ctx, h)
 
     def release(self):
         """Gives up ownership (the C side took it)."""
@@ -359,6 +375,30 @@ def pcg(ctx, A, b, x=None, precon=None, tol=1e-8, maxit=200):
     return x, hist[:it.value].copy()
 
 
+def h_interp(ctx, n_fine, P):
+    """One level of InterpolationHierarchy<2,P>: (n_fine/2)^2 -> n_fine^2 elements."""
+    h = C.c_void_p()
+    ctx.check(lib().mgldg_cartesian_h_interp(ctx.h, n_fine, P, C.byref(h)), "h_interp")
+    return SparseBlockMatrix(ctx, h)
+
+
+def p_interp(ctx, ne, P_fine, P_coarse):
+    """InterpolationHierarchy<2,Pf,Pc>: degree Pc -> Pf on the same ne elements."""
+    h = C.c_void_p()
+    ctx.check(lib().mgldg_cartesian_p_interp(ctx.h, ne, P_fine, P_coarse, C.byref(h)), "p_interp")
+    return SparseBlockMatrix(ctx, h)
+
+
+def hp_chain(ctx, n, degrees, nh):
+    """Transfers of Multigrid<2,P1,P2,...>: p-levels over `degrees`, then nh h-levels."""
+    T = [p_interp(ctx, n * n, degrees[k - 1], degrees[k]) for k in range(1, len(degrees))]
+    nf = n
+    for _ in range(nh):
+        T.append(h_interp(ctx, nf, degrees[-1]))
+        nf //= 2
+    return T
+
+
 class CartesianProblem:
     """Uniform n x n quadtree mesh, Q_{P-1} LDG operators and hierarchy, built on the GPU."""
 
@@ -380,6 +420,11 @@ class CartesianProblem:
             t = C.c_void_p()
             ctx.check(lib().mgldg_problem_interp(h, l, C.byref(t)), "problem_interp")
             self.T.append(SparseBlockMatrix(ctx, t, owned=False))
+
+    def write_fun(self, u, path):
+        """Nodal dump of u (the reference's Function::write format)."""
+        self.ctx.check(lib().mgldg_problem_write_fun(self.ctx.h, self.h, np.ascontiguousarray(u, np.float64),
+                                                     str(path).encode()), "write_fun")
 
     def rhs_gaussian(self, seed):
         b = np.zeros(self.ndof)

@@ -24,7 +24,9 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <fstream>
 #include <functional>
+#include <limits>
 #include <memory>
 #include <random>
 #include <stdexcept>
@@ -951,18 +953,19 @@ static void discretize(Problem& pr, std::vector<double>& rhs) {
     }
 }
 
-// InterpolationHierarchy<N,P> (interpolationhierarchy.h:30-82)
-static void build_hierarchy(Problem& pr) {
-    const Quadtree& qt = *pr.qt;
-    int P = pr.P, npl = pr.npl;
+// InterpolationHierarchy<N,P> (interpolationhierarchy.h:30-82), for any
+// degree P on the problem's quadtree
+static std::vector<SBM> h_hierarchy(const Quadtree& qt, int P) {
+    std::vector<SBM> out;
+    int npl = P * P;
     const Tables& T = tables(P);
     for (int l = 0; l < qt.numLevels - 1; ++l) {
         std::vector<int> fine = qt.layer(l), coarse = qt.layer(l + 1);
         std::unordered_map<int, int> cg2l;
         int clid = 0;
         for (int g : coarse) cg2l[g] = clid++;
-        pr.hier.emplace_back((int)fine.size(), (int)coarse.size(), npl, npl);
-        SBM& Tm = pr.hier.back();
+        out.emplace_back((int)fine.size(), (int)coarse.size(), npl, npl);
+        SBM& Tm = out.back();
         int flid = 0;
         for (int fg : fine) {
             if (qt.isLeaf(qt.tree[fg], l + 1)) {
@@ -990,6 +993,27 @@ static void build_hierarchy(Problem& pr) {
             }
         }
     }
+    return out;
+}
+
+static void build_hierarchy(Problem& pr) { pr.hier = h_hierarchy(*pr.qt, pr.P); }
+
+// p-interpolation from degree P2 to degree P1 on the same elements
+// (InterpolationHierarchy<N,P1,P2>, interpolationhierarchy.h:109-129): the
+// block-diagonal operator whose block evaluates the P2 Lagrange basis at the
+// P1 nodes of the master element
+static SBM p_transfer(int ne, int P1, int P2) {
+    int b1 = P1 * P1, b2 = P2 * P2;
+    const Tables& T1 = tables(P1);
+    Mat E(b1, b2);
+    for (int i0 = 0; i0 < P1; ++i0)
+        for (int i1 = 0; i1 < P1; ++i1) {
+            double node[2] = {T1.nodes[i0], T1.nodes[i1]};
+            lagrange2(P2, node, &E(i0 * P1 + i1, 0));
+        }
+    SBM Tm(ne, ne, b1, b2);
+    for (int i = 0; i < ne; ++i) Tm.set(i, i, E);
+    return Tm;
 }
 
 // Gaussian-sum forcing: 8 Gaussians, centres U[0,1]^2, widths U[0.05,0.2],
@@ -1118,6 +1142,7 @@ struct MG {
     bool mean_project;
     const Problem* pr;
     std::vector<std::unique_ptr<Level>> levels;
+    std::vector<SBM> Ts;   // Ts[i] interpolates level i+1 to level i
 
     // Level(fineOps) (multigrid.h:83-96)
     void fine_level(std::shared_ptr<Ops> ops) {
@@ -1285,10 +1310,10 @@ struct MG {
             relax(L, npre, false);
             computeResidual(L);
             Level& C = *levels[i + 1];
-            multiply_mv_t(pr->hier[i], L.r.data(), C.b.data());   // restrictResidual :414-418
+            multiply_mv_t(Ts[i], L.r.data(), C.b.data());   // restrictResidual :414-418
             std::fill(C.x.begin(), C.x.end(), 0.0);
             vcycle(i + 1);
-            multiply_add_mv(1.0, pr->hier[i], C.x.data(), 1.0, L.x.data());   // correctSolution :421-425
+            multiply_add_mv(1.0, Ts[i], C.x.data(), 1.0, L.x.data());   // correctSolution :421-425
             relax(L, npost, true);
         }
     }
@@ -1498,10 +1523,52 @@ int orc_mg_create(const orc_problem* pr, int relaxation, double omega, int solve
         m->fine_level(pr->p->ops);
         int nT = (int)pr->p->hier.size();
         int use = (nlevels <= 0) ? nT : std::min(nT, nlevels - 1);
-        for (int i = 0; i < use; ++i) m->coarse_level(*m->levels[i]->ops, pr->p->hier[i]);
+        for (int i = 0; i < use; ++i) m->Ts.push_back(pr->p->hier[i]);
+        for (int i = 0; i < use; ++i) m->coarse_level(*m->levels[i]->ops, m->Ts[i]);
         if (solver == ORC_COARSE_DENSE) m->dense_factor(*m->levels.back());
         *out = new orc_mg{m.release()};
     })
+}
+
+// hp-multigrid (Multigrid<N,P1,P2,...>, multigrid.h:436-560): p-levels
+// degrees[0] (the problem's P) -> degrees[1] -> ... on the fine mesh, then
+// nh h-levels at the last degree (InterpolationHierarchy<N,Pk>)
+int orc_mg_create_hp(const orc_problem* pr, const int* degrees, int ndeg, int nh, int relaxation, double omega,
+                     int solver, int npre, int npost, int restriction, int mean_project, orc_mg** out) {
+    ORC_TRY({
+        const Problem& p = *pr->p;
+        if (ndeg < 1 || degrees[0] != p.P) throw std::invalid_argument("degrees[0] must be the problem's P");
+        std::unique_ptr<MG> m(new MG());
+        m->relaxation = relaxation; m->omega = omega; m->solver = solver;
+        m->npre = npre; m->npost = npost; m->restriction = restriction;
+        m->mean_project = mean_project != 0;
+        m->pr = pr->p;
+        m->fine_level(p.ops);
+        const int ne = (int)p.mesh->elements.size();
+        for (int k = 1; k < ndeg; ++k) m->Ts.push_back(p_transfer(ne, degrees[k - 1], degrees[k]));
+        if (nh > 0) {
+            std::vector<SBM> h = h_hierarchy(*p.qt, degrees[ndeg - 1]);
+            for (int i = 0; i < nh && i < (int)h.size(); ++i) m->Ts.push_back(h[i]);
+        }
+        for (size_t i = 0; i < m->Ts.size(); ++i) m->coarse_level(*m->levels[i]->ops, m->Ts[i]);
+        if (solver == ORC_COARSE_DENSE) m->dense_factor(*m->levels.back());
+        *out = new orc_mg{m.release()};
+    })
+}
+
+// T[l] of the hp hierarchy built by orc_mg_create_hp / orc_mg_create
+int orc_mg_transfer_shape(const orc_mg* mg, int l, int* nbr, int* nbc, int* br, int* bc, int* nnzb) {
+    ORC_TRY({
+        const SBM& T = mg->m->Ts.at(l);
+        if (nbr) *nbr = T.blockRows();
+        if (nbc) *nbc = T.blockCols();
+        if (br) *br = T.P;
+        if (bc) *bc = T.Q;
+        if (nnzb) *nnzb = (int)T.nnzb();
+    })
+}
+int orc_mg_transfer_export(const orc_mg* mg, int l, int* row_ptr, int* col_idx, double* vals) {
+    ORC_TRY({ export_csr(mg->m->Ts.at(l), row_ptr, col_idx, vals); })
 }
 int orc_mg_destroy(orc_mg* mg) {
     if (mg) { delete mg->m; delete mg; }
@@ -1563,6 +1630,44 @@ int orc_pcg(const orc_problem* pr, orc_mg* mg, const double* b, double* x, doubl
         if (iters) *iters = it;
     })
 }
+// SparseBlockMatrix::write (sparseblockmatrix.tpp:145-164): block-map order
+int orc_problem_write_mtx(const orc_problem* pr, int which, const char* path) {
+    ORC_TRY({
+        const SBM& A = op_of(*pr->p->ops, which);
+        std::ofstream ofs(path);
+        ofs.precision(std::numeric_limits<double>::max_digits10);
+        ofs << "%%MatrixMarket matrix coordinate real general" << std::endl;
+        ofs << A.rows() << " " << A.cols() << " " << (long)A.P * A.Q * A.nnzb() << std::endl;
+        for (auto it = A.map.begin(); it != A.map.end(); ++it) {
+            int bi = it->first.i * A.P, bj = it->first.j * A.Q;
+            for (int i = 0; i < A.P; ++i)
+                for (int j = 0; j < A.Q; ++j) ofs << bi + i + 1 << " " << bj + j + 1 << " " << it->second(i, j) << std::endl;
+        }
+        if (!ofs) throw std::runtime_error("write failed");
+    })
+}
+// Function::write (function.h:173-190)
+int orc_problem_write_fun(const orc_problem* pr, const double* u, const char* path) {
+    ORC_TRY({
+        const Problem& p = *pr->p;
+        const Tables& T = tables(p.P);
+        std::ofstream ofs(path);
+        ofs.precision(std::numeric_limits<double>::max_digits10);
+        int ne = (int)p.mesh->elements.size();
+        ofs << p.P << " " << NDIM << " " << ne << std::endl;
+        for (int e = 0; e < ne; ++e) {
+            const Cell& c = p.mesh->elements[e];
+            for (int i0 = 0; i0 < p.P; ++i0)
+                for (int i1 = 0; i1 < p.P; ++i1) {
+                    double x = c.lo[0] + c.width(0) * T.nodes[i0], y = c.lo[1] + c.width(1) * T.nodes[i1];
+                    ofs << x << " " << y << " " << u[(size_t)e * p.npl + i0 * p.P + i1] << std::endl;
+                }
+            ofs << std::endl;
+        }
+        if (!ofs) throw std::runtime_error("write failed");
+    })
+}
+
 int orc_problem_mv(const orc_problem* pr, int which, double alpha, const double* x, double beta, double* y) {
     ORC_TRY({ multiply_add_mv(alpha, op_of(*pr->p->ops, which), x, beta, y); })
 }

@@ -90,6 +90,14 @@ enum { ORC_RESTRICT_RAT = 0, ORC_RESTRICT_RATRAT = 1 };
 int orc_mg_create(const orc_problem* pr, int relaxation, double omega, int solver,
                   int npre, int npost, int restriction, int nlevels,
                   int mean_project, orc_mg** out);
+/* hp-multigrid (multigrid.h:436-560): p-levels degrees[0] (= the problem's
+ * P) -> ... -> degrees[ndeg-1] on the fine mesh, then nh h-levels at the
+ * last degree.  Transfers are kept by the mg handle. */
+int orc_mg_create_hp(const orc_problem* pr, const int* degrees, int ndeg, int nh, int relaxation,
+                     double omega, int solver, int npre, int npost, int restriction,
+                     int mean_project, orc_mg** out);
+int orc_mg_transfer_shape(const orc_mg* mg, int l, int* nbr, int* nbc, int* br, int* bc, int* nnzb);
+int orc_mg_transfer_export(const orc_mg* mg, int l, int* row_ptr, int* col_idx, double* vals);
 int orc_mg_destroy(orc_mg* mg);
 int orc_mg_nlevels(const orc_mg* mg, int* n);
 /* level operator export: which 0=M 1=G0 2=G1 3=T 4=A */
@@ -104,6 +112,11 @@ int orc_mg_relax(orc_mg* mg, int l, int n, int reverse, const double* b, double*
  * hist[k] = ||r|| printed after iteration k (needs maxit doubles). */
 int orc_pcg(const orc_problem* pr, orc_mg* mg, const double* b, double* x,
             double tol, int maxit, int* iters, double* hist, double* delta_hist);
+/* Matrix Market dump of a fine-level operator (SparseBlockMatrix::write,
+ * sparseblockmatrix.tpp:145-164) and nodal dump of a vector
+ * (Function::write, function.h:173-190). */
+int orc_problem_write_mtx(const orc_problem* pr, int which, const char* path);
+int orc_problem_write_fun(const orc_problem* pr, const double* u, const char* path);
 /* y := alpha*A*x + beta*y with the fine-level operator `which` */
 int orc_problem_mv(const orc_problem* pr, int which, double alpha, const double* x,
                    double beta, double* y);

@@ -65,6 +65,10 @@ def lib():
         L.orc_mg_create.argtypes = [vp, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
                                     C.c_int, C.c_int, pvp]
         L.orc_mg_destroy.argtypes = [vp]
+        L.orc_mg_create_hp.argtypes = [vp, _ip, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int,
+                                       C.c_int, C.c_int, pvp]
+        L.orc_mg_transfer_shape.argtypes = [vp, C.c_int, ip, ip, ip, ip, ip]
+        L.orc_mg_transfer_export.argtypes = [vp, C.c_int, _ip, _ip, _dp]
         L.orc_mg_nlevels.argtypes = [vp, ip]
         L.orc_mg_level_nnzb.argtypes = [vp, C.c_int, C.c_int, ip, ip]
         L.orc_mg_level_export.argtypes = [vp, C.c_int, C.c_int, _ip, _ip, _dp]
@@ -72,6 +76,8 @@ def lib():
         L.orc_mg_relax.argtypes = [vp, C.c_int, C.c_int, C.c_int, _dp, _dp]
         L.orc_pcg.argtypes = [vp, vp, _dp, _dp, C.c_double, C.c_int, ip, _dp, _dp]
         L.orc_problem_mv.argtypes = [vp, C.c_int, C.c_double, _dp, C.c_double, _dp]
+        L.orc_problem_write_mtx.argtypes = [vp, C.c_int, C.c_char_p]
+        L.orc_problem_write_fun.argtypes = [vp, _dp, C.c_char_p]
         _lib = L
     return _lib
 
@@ -221,6 +227,12 @@ class Problem:
                            v.reshape(-1, self.npl, self.npl)))
         return out
 
+    def write_mtx(self, which, path):
+        _ck(lib().orc_problem_write_mtx(self.h, which, str(path).encode()), "write_mtx")
+
+    def write_fun(self, u, path):
+        _ck(lib().orc_problem_write_fun(self.h, np.ascontiguousarray(u, np.float64), str(path).encode()), "write_fun")
+
     def mv(self, which, x, alpha=1.0, beta=0.0, y=None):
         y = np.zeros(self.ndof) if y is None else np.array(y, dtype=np.float64)
         _ck(lib().orc_problem_mv(self.h, which, alpha, np.ascontiguousarray(x, np.float64), beta, y), "mv")
@@ -253,6 +265,32 @@ class Multigrid:
         if getattr(self, "h", None) and _lib is not None:
             _lib.orc_mg_destroy(self.h)
             self.h = None
+
+    @classmethod
+    def hp(cls, problem, degrees, nh, relaxation=RELAX_GS, omega=0.8, solver=COARSE_CHOLESKY, npre=3, npost=3,
+           restriction=RESTRICT_RATRAT, mean_project=True):
+        """Multigrid<N,P1,P2,...>: p-levels over `degrees`, then nh h-levels."""
+        self = cls.__new__(cls)
+        h = C.c_void_p()
+        deg = np.ascontiguousarray(degrees, dtype=np.int32)
+        _ck(lib().orc_mg_create_hp(problem.h, deg, len(deg), nh, relaxation, omega, solver, npre, npost,
+                                   restriction, int(mean_project), C.byref(h)), "mg_create_hp")
+        self.h, self.pr = h, problem
+        n = C.c_int()
+        _ck(lib().orc_mg_nlevels(h, C.byref(n)), "nlevels")
+        self.nlevels = n.value
+        return self
+
+    def transfer(self, l):
+        """T[l]: interpolation from level l+1 to level l."""
+        v = [C.c_int() for _ in range(5)]
+        _ck(lib().orc_mg_transfer_shape(self.h, l, *[C.byref(x) for x in v]), "transfer_shape")
+        nbr, nbc, br, bc, nnzb = [x.value for x in v]
+        rp = np.zeros(nbr + 1, np.int32)
+        ci = np.zeros(max(1, nnzb), np.int32)
+        vals = np.zeros(max(1, nnzb * br * bc))
+        _ck(lib().orc_mg_transfer_export(self.h, l, rp, ci, vals), "transfer_export")
+        return CSR(nbr, nbc, br, bc, rp, ci[:nnzb], vals[:nnzb * br * bc].reshape(-1, br, bc))
 
     def level_op(self, l, which):
         nbr, nnzb = C.c_int(), C.c_int()

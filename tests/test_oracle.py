@@ -139,6 +139,21 @@ def test_adaptive_mesh_with_hanging_faces():
     assert hist[-1] < 1e-8 * max(1.0, hist[0])
 
 
+@pytest.mark.parametrize("degrees,nh", [([4, 2], 3), ([4, 3, 2], 3)])
+def test_hp_multigrid_converges_and_transfers_interpolate(degrees, nh):
+    # Multigrid<N,P1,P2,...> (multigrid.h:436-560): p-levels, then h-levels
+    pr = O.Problem(degrees[0], 1 / 16, seed=1001)
+    mg = O.Multigrid.hp(pr, degrees, nh, npre=2, npost=2, solver=O.COARSE_DENSE, mean_project=False)
+    assert mg.nlevels == len(degrees) + nh
+    for l in range(mg.nlevels - 1):
+        T = mg.transfer(l)
+        assert np.allclose(T.matvec(np.ones(T.nbc * T.bc)), 1.0, atol=1e-13)
+    x, hist, _ = pr.pcg(pr.rhs(), mg=mg, tol=1e-10)
+    assert len(hist) < 30
+    u = np.linalg.solve(pr.op(O.OP_A).todense(), pr.rhs())
+    assert np.abs(x - u).max() <= 1e-8 * np.abs(u).max()
+
+
 def test_gaussian_params_deterministic():
     a = O.gaussian_params(1001)
     b = O.gaussian_params(1001)
