@@ -1584,6 +1584,9 @@ int orc_mg_level_nnzb(const orc_mg* mg, int l, int which, int* nbr, int* nnzb) {
         if (nnzb) *nnzb = (int)A.nnzb();
     })
 }
+int orc_mg_level_block(const orc_mg* mg, int l, int* b) {
+    ORC_TRY({ *b = mg->m->levels.at(l)->npl; })
+}
 int orc_mg_level_export(const orc_mg* mg, int l, int which, int* row_ptr, int* col_idx, double* vals) {
     ORC_TRY({ export_csr(op_of(*mg->m->levels.at(l)->ops, which), row_ptr, col_idx, vals); })
 }

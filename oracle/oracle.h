@@ -102,6 +102,7 @@ int orc_mg_destroy(orc_mg* mg);
 int orc_mg_nlevels(const orc_mg* mg, int* n);
 /* level operator export: which 0=M 1=G0 2=G1 3=T 4=A */
 int orc_mg_level_nnzb(const orc_mg* mg, int l, int which, int* nbr, int* nnzb);
+int orc_mg_level_block(const orc_mg* mg, int l, int* b);   /* block size of level l */
 int orc_mg_level_export(const orc_mg* mg, int l, int which, int* row_ptr,
                         int* col_idx, double* vals);
 /* one V-cycle from level 0: x (in/out) with right-hand side b */

@@ -72,6 +72,7 @@ def lib():
         L.orc_mg_nlevels.argtypes = [vp, ip]
         L.orc_mg_level_nnzb.argtypes = [vp, C.c_int, C.c_int, ip, ip]
         L.orc_mg_level_export.argtypes = [vp, C.c_int, C.c_int, _ip, _ip, _dp]
+        L.orc_mg_level_block.argtypes = [vp, C.c_int, ip]
         L.orc_mg_vcycle.argtypes = [vp, _dp, _dp]
         L.orc_mg_relax.argtypes = [vp, C.c_int, C.c_int, C.c_int, _dp, _dp]
         L.orc_pcg.argtypes = [vp, vp, _dp, _dp, C.c_double, C.c_int, ip, _dp, _dp]
@@ -295,7 +296,9 @@ class Multigrid:
     def level_op(self, l, which):
         nbr, nnzb = C.c_int(), C.c_int()
         _ck(lib().orc_mg_level_nnzb(self.h, l, which, C.byref(nbr), C.byref(nnzb)), "lnnzb")
-        b = self.pr.npl
+        bb = C.c_int()
+        _ck(lib().orc_mg_level_block(self.h, l, C.byref(bb)), "lblock")
+        b = bb.value
         rp = np.zeros(nbr.value + 1, np.int32)
         ci = np.zeros(nnzb.value, np.int32)
         v = np.zeros(nnzb.value * b * b)
