@@ -223,6 +223,29 @@ int mgldg_bsr_read_mtx(mgldg_ctx* ctx, const char* path, int br, int bc, mgldg_b
  * one "x y value" line per node and an empty line. */
 int mgldg_problem_write_fun(mgldg_ctx* ctx, const mgldg_problem* pr, const double* u, const char* path);
 
+/* ------------------------------------------- diffusivity and adjoints -- */
+/* No counterpart in the reference (its operators have unit diffusivity);
+ * these entries extend construct_laplacian (ldgpoisson.h:34-52) and the pcg
+ * of krylov.h:22-68 to a per-element diffusivity kappa and its adjoint.
+ *
+ * A = T + sum_d G_d^T diag(kappa_e M_e) G_d, replacing ops' Laplacian.
+ * kappa: host array, one positive value per element (row of M), or NULL
+ * for kappa = 1 (then A equals mgldg_ops_construct_laplacian's). */
+int mgldg_ops_construct_laplacian_kappa(mgldg_ctx* ctx, mgldg_ops* ops, const double* kappa);
+/* dkappa[e] = -sum_d (G_d lambda)_e^T M_e (G_d u)_e  (device vectors):
+ * the gradient of a loss L with respect to kappa_e when A(kappa) u = b and
+ * lambda solves the adjoint system A lambda = dL/du. */
+int mgldg_kappa_gradient_dev(mgldg_ctx* ctx, const mgldg_ops* ops, const double* u,
+                             const double* lambda, double* dkappa);
+/* Loss L = 1/2 ||u - u_obs||^2 of the solution of ops' A u = b: forward pcg
+ * (u in/out, the initial guess on entry), adjoint pcg with the same
+ * preconditioner mg (lambda in/out) and, if dkappa != NULL, dL/dkappa.
+ * dL/db = lambda.  loss (host, may be NULL); iters[2] (host, may be NULL) =
+ * forward and adjoint iteration counts.  All vectors are device pointers. */
+int mgldg_adjoint_l2_dev(mgldg_ctx* ctx, mgldg_mg* mg, const mgldg_ops* ops, const double* b,
+                         const double* u_obs, double tol, int maxit, double* u, double* lambda,
+                         double* dkappa, double* loss, int* iters);
+
 /* ------------------------------------------------------------ host logic -- */
 /* Level sets of the block Gauss-Seidel sweep (host only, no GPU needed): for
  * the forward sweep of multigrid.h:240-249 (reverse=0) or the reverse sweep

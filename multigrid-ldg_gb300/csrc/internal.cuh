@@ -166,6 +166,8 @@ void finish_sum(mgldg_ctx* ctx, const double* partials, int npart, double* out);
 
 // setup.cu
 void construct_laplacian(mgldg_ctx* ctx, mgldg_ops* ops);
+// T + sum_d G_d^T M G_d for a block-diagonal M (new matrix)
+mgldg_bsr* laplacian_of(mgldg_ctx* ctx, mgldg_bsr* M, mgldg_bsr* const* G, int ndim, mgldg_bsr* T);
 void block_inverse(mgldg_ctx* ctx, const mgldg_bsr* A, double* out, int* status);
 mgldg_ops* galerkin_ratrat(mgldg_ctx* ctx, const mgldg_ops* f, const mgldg_bsr* T);
 mgldg_ops* galerkin_rat(mgldg_ctx* ctx, const mgldg_ops* f, const mgldg_bsr* T);

@@ -422,6 +422,10 @@ static mgldg_bsr* laplacian(mgldg_ctx* ctx, mgldg_bsr* M, mgldg_bsr* const* G, i
     return A;
 }
 
+mgldg_bsr* laplacian_of(mgldg_ctx* ctx, mgldg_bsr* M, mgldg_bsr* const* G, int ndim, mgldg_bsr* T) {
+    return laplacian(ctx, M, G, ndim, T);
+}
+
 void construct_laplacian(mgldg_ctx* ctx, mgldg_ops* ops) {
     MG_REQUIRE(ops->has_MGT(), MGLDG_ERR_ARG, "construct_laplacian needs M, G and T");
     mgldg_bsr* A = laplacian(ctx, ops->M, ops->G, ops->ndim, ops->T);

@@ -37,6 +37,7 @@ EXPORTS = [
     "mgldg_prof_query", "mgldg_gs_levels", "mgldg_selftest_wait_timeout", "mgldg_cg_noalloc_dev",
     "mgldg_prof_query_level", "mgldg_cartesian_h_interp", "mgldg_cartesian_p_interp",
     "mgldg_bsr_write_mtx", "mgldg_bsr_read_mtx", "mgldg_problem_write_fun",
+    "mgldg_ops_construct_laplacian_kappa", "mgldg_kappa_gradient_dev", "mgldg_adjoint_l2_dev",
 ]
 
 
@@ -134,6 +135,10 @@ def lib():
         L.mgldg_bsr_write_mtx.argtypes = [vp, vp, C.c_char_p]
         L.mgldg_bsr_read_mtx.argtypes = [vp, C.c_char_p, C.c_int, C.c_int, pvp]
         L.mgldg_problem_write_fun.argtypes = [vp, vp, _dp, C.c_char_p]
+        L.mgldg_ops_construct_laplacian_kappa.argtypes = [vp, vp, vp]
+        L.mgldg_kappa_gradient_dev.argtypes = [vp, vp, vp, vp, vp]
+        L.mgldg_adjoint_l2_dev.argtypes = [vp, vp, vp, vp, vp, C.c_double, C.c_int, vp, vp, vp,
+                                           C.POINTER(C.c_double), ip]
         _lib = L
     return _lib
 
@@ -296,6 +301,12 @@ class LDGOperators:
     def construct_laplacian(self):
         self.ctx.check(lib().mgldg_ops_construct_laplacian(self.ctx.h, self.h), "construct_laplacian")
 
+    def construct_laplacian_kappa(self, kappa=None):
+        """A = T + sum_d G_d^T diag(kappa_e M_e) G_d (kappa: one value per element, None = 1)."""
+        k = None if kappa is None else np.ascontiguousarray(kappa, np.float64)
+        ptr = None if k is None else k.ctypes.data_as(C.c_void_p)
+        self.ctx.check(lib().mgldg_ops_construct_laplacian_kappa(self.ctx.h, self.h, ptr), "construct_laplacian_kappa")
+
     def get(self, which):
         out = C.c_void_p()
         self.ctx.check(lib().mgldg_ops_get(self.h, which, C.byref(out)), "ops_get")
@@ -373,6 +384,47 @@ def pcg(ctx, A, b, x=None, precon=None, tol=1e-8, maxit=200):
     rc = lib().mgldg_pcg(ctx.h, precon.h if precon is not None else None, A.h, b, x, tol, maxit, C.byref(it), hist)
     ctx.check(rc, "pcg")
     return x, hist[:it.value].copy()
+
+
+def _device_vectors(*arrays):
+    """float64 CUDA copies of host arrays (device memory comes from torch)."""
+    import torch
+    return [torch.from_numpy(np.ascontiguousarray(a, np.float64)).to("cuda") for a in arrays]
+
+
+def adjoint_l2(ctx, ops, b, u_obs, precon=None, tol=1e-10, maxit=200, u0=None):
+    """L = 1/2 ||u - u_obs||^2 with A u = b (ops' Laplacian): forward and adjoint pcg
+    with the same preconditioner, then dL/dkappa.  Returns
+    (u, lambda = dL/db, dL/dkappa, L, (forward iterations, adjoint iterations))."""
+    import torch
+    b = np.ascontiguousarray(b, np.float64)
+    n = len(b)
+    ne = n // (ops.get(0).info()[2])
+    db, dobs, du = _device_vectors(b, u_obs, np.zeros(n) if u0 is None else u0)
+    dl = torch.zeros(n, dtype=torch.float64, device="cuda")
+    dk = torch.zeros(max(1, ne), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    loss = C.c_double()
+    its = (C.c_int * 2)()
+    p = lambda t: C.c_void_p(t.data_ptr())
+    rc = lib().mgldg_adjoint_l2_dev(ctx.h, precon.h if precon is not None else None, ops.h, p(db), p(dobs), tol,
+                                    maxit, p(du), p(dl), p(dk), C.byref(loss), its)
+    ctx.check(rc, "adjoint_l2")
+    ctx.sync()
+    return (du.cpu().numpy(), dl.cpu().numpy(), dk.cpu().numpy()[:ne], loss.value, (its[0], its[1]))
+
+
+def kappa_gradient(ctx, ops, u, lam):
+    """dL/dkappa_e = -sum_d (G_d lam)_e^T M_e (G_d u)_e for host vectors u, lam."""
+    import torch
+    du, dl = _device_vectors(u, lam)
+    ne = len(u) // (ops.get(0).info()[2])
+    dk = torch.zeros(max(1, ne), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    p = lambda t: C.c_void_p(t.data_ptr())
+    ctx.check(lib().mgldg_kappa_gradient_dev(ctx.h, ops.h, p(du), p(dl), p(dk)), "kappa_gradient")
+    ctx.sync()
+    return dk.cpu().numpy()[:ne]
 
 
 def h_interp(ctx, n_fine, P):
