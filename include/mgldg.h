@@ -223,6 +223,35 @@ int mgldg_bsr_read_mtx(mgldg_ctx* ctx, const char* path, int br, int bc, mgldg_b
  * one "x y value" line per node and an empty line. */
 int mgldg_problem_write_fun(mgldg_ctx* ctx, const mgldg_problem* pr, const double* u, const char* path);
 
+/* ------------------------------------------- many right-hand sides -- */
+/* No counterpart in the reference (it solves one right-hand side at a time
+ * with pcg, krylov.h:22-68).  A multi-vector of k columns (1 <= k <= 1024)
+ * over n unknowns is row-major: X[u*k + c].
+ *
+ * Y := alpha*A*X + beta*Y on device multi-vectors (multiply_add_mv,
+ * sparseblockmatrix.tpp:358-371, applied to k vectors at once). */
+int mgldg_bsr_mm_dev(mgldg_ctx* ctx, double alpha, const mgldg_bsr* A, int k,
+                     const double* X, double beta, double* Y);
+/* One V-cycle per column (vcycle, multigrid.h:361-383) with X as the initial
+ * guess (in/out).  Needs params.relaxation == MGLDG_RELAX_JACOBI. */
+int mgldg_mg_vcycle_batched_dev(mgldg_ctx* ctx, mgldg_mg* mg, int k, const double* B, double* X);
+/* pcg (krylov.h:22-68) on every column of B at once, sharing each SpMM and
+ * V-cycle; column c stops on its own criterion and equals the single-RHS
+ * solve of B[:,c].  iters[k] (host, may be NULL); res_hist (host, may be
+ * NULL) receives maxit*k doubles, res_hist[c*maxit + i] = ||r_c|| after
+ * iteration i.  MGLDG_ERR_BREAKDOWN names the first broken column.  The
+ * column tile of every SpMM is autotuned on the first call for a given k. */
+int mgldg_pcg_batched_dev(mgldg_ctx* ctx, mgldg_mg* mg, const mgldg_bsr* A, int k,
+                          const double* B, double* X, double tol, int maxit, int* iters,
+                          double* res_hist);
+int mgldg_pcg_batched(mgldg_ctx* ctx, mgldg_mg* mg, const mgldg_bsr* A, int k,
+                      const double* B, double* X, double tol, int maxit, int* iters,
+                      double* res_hist);
+/* Column tile widths (32, 64 or 128) the autotuner chose for level `level`'s
+ * SpMM, Jacobi sweep, restriction, prolongation and for the outer FP64 SpMM. */
+int mgldg_mg_batch_tiles(const mgldg_mg* mg, int level, int* spmm, int* jacobi, int* restrict_,
+                         int* prolong, int* outer);
+
 /* ------------------------------------------- diffusivity and adjoints -- */
 /* No counterpart in the reference (its operators have unit diffusivity);
  * these entries extend construct_laplacian (ldgpoisson.h:34-52) and the pcg

@@ -16,78 +16,9 @@
 #include <string>
 
 #include "api.cuh"
-#include "smooth.cuh"
+#include "mg.cuh"
 
 using namespace mg;
-
-namespace mg {
-
-struct LevelData {
-    mgldg_ops* ops = nullptr;    // owned for coarse levels
-    bool owns_ops = false;
-    const mgldg_bsr* A = nullptr;
-    int ne = 0, b = 0;
-    int64_t n = 0;
-    double* Dinv = nullptr;
-    float* Dinv32 = nullptr;
-    Sched sched;
-    bool has_sched = false;
-    double *x = nullptr, *bb = nullptr, *r = nullptr, *xt = nullptr;
-    float *x32 = nullptr, *b32 = nullptr, *r32 = nullptr, *xt32 = nullptr;
-    mgldg_bsr* T = nullptr;    // interpolation to this level from the next coarser one
-    mgldg_bsr* Tt = nullptr;   // its transpose (restriction)
-};
-
-template <class T>
-struct LV;
-template <>
-struct LV<double> {
-    static double*& x(LevelData& L) { return L.x; }
-    static double*& b(LevelData& L) { return L.bb; }
-    static double*& r(LevelData& L) { return L.r; }
-    static double*& xt(LevelData& L) { return L.xt; }
-    static const double* D(LevelData& L) { return L.Dinv; }
-};
-template <>
-struct LV<float> {
-    static float*& x(LevelData& L) { return L.x32; }
-    static float*& b(LevelData& L) { return L.b32; }
-    static float*& r(LevelData& L) { return L.r32; }
-    static float*& xt(LevelData& L) { return L.xt32; }
-    static const float* D(LevelData& L) { return L.Dinv32; }
-};
-
-struct PcgScalars {
-    double delta_new, delta_old, delta0, alpha, beta, dq, rr, pad;
-    int breakdown, pad2[3];
-};
-
-}  // namespace mg
-
-struct mgldg_mg {
-    mgldg_ctx* ctx = nullptr;
-    mgldg_mg_params p;
-    std::vector<mg::LevelData> L;
-    double* Cinv = nullptr;   // dense inverse of the coarsest matrix
-    int nc = 0;
-    // pcg work space
-    double *r = nullptr, *d = nullptr, *q = nullptr, *s = nullptr, *hist = nullptr;
-    int64_t pcg_n = 0;
-    int pcg_maxit = 0;
-    mg::PcgScalars* sc = nullptr;
-    mg::PcgScalars* h_sc = nullptr;   // pinned
-    // preconditioner V-cycles captured as CUDA graphs, keyed by (in, out)
-    struct Graph {
-        const double* in = nullptr;
-        double* out = nullptr;
-        cudaGraphExec_t exec = nullptr;
-        int64_t launches[MGLDG_K_NCLASS] = {0};
-    };
-    Graph graphs[2];
-    int next_graph = 0;
-    bool graphs_off = false;
-    ~mgldg_mg();
-};
 
 namespace mg {
 
@@ -541,6 +472,7 @@ mgldg_mg::~mgldg_mg() {
     dfree(r); dfree(d); dfree(q); dfree(s); dfree(hist);
     dfree(sc);
     if (h_sc) cudaFreeHost(h_sc);
+    mg::batch_free(batch);
 }
 
 // ================================================================== C ABI ==

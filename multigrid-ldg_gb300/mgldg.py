@@ -38,6 +38,8 @@ EXPORTS = [
     "mgldg_prof_query_level", "mgldg_cartesian_h_interp", "mgldg_cartesian_p_interp",
     "mgldg_bsr_write_mtx", "mgldg_bsr_read_mtx", "mgldg_problem_write_fun",
     "mgldg_ops_construct_laplacian_kappa", "mgldg_kappa_gradient_dev", "mgldg_adjoint_l2_dev",
+    "mgldg_bsr_mm_dev", "mgldg_mg_vcycle_batched_dev", "mgldg_pcg_batched_dev", "mgldg_pcg_batched",
+    "mgldg_mg_batch_tiles",
 ]
 
 
@@ -139,6 +141,11 @@ def lib():
         L.mgldg_kappa_gradient_dev.argtypes = [vp, vp, vp, vp, vp]
         L.mgldg_adjoint_l2_dev.argtypes = [vp, vp, vp, vp, vp, C.c_double, C.c_int, vp, vp, vp,
                                            C.POINTER(C.c_double), ip]
+        L.mgldg_bsr_mm_dev.argtypes = [vp, C.c_double, vp, C.c_int, vp, C.c_double, vp]
+        L.mgldg_mg_vcycle_batched_dev.argtypes = [vp, vp, C.c_int, vp, vp]
+        L.mgldg_pcg_batched_dev.argtypes = [vp, vp, vp, C.c_int, vp, vp, C.c_double, C.c_int, _ip, _dp]
+        L.mgldg_pcg_batched.argtypes = [vp, vp, vp, C.c_int, _dp, _dp, C.c_double, C.c_int, _ip, _dp]
+        L.mgldg_mg_batch_tiles.argtypes = [vp, C.c_int, ip, ip, ip, ip, ip]
         _lib = L
     return _lib
 
@@ -384,6 +391,29 @@ def pcg(ctx, A, b, x=None, precon=None, tol=1e-8, maxit=200):
     rc = lib().mgldg_pcg(ctx.h, precon.h if precon is not None else None, A.h, b, x, tol, maxit, C.byref(it), hist)
     ctx.check(rc, "pcg")
     return x, hist[:it.value].copy()
+
+
+def pcg_batched(ctx, A, B, X=None, precon=None, tol=1e-8, maxit=200):
+    """pcg on the k columns of B (n x k) at once; returns (X, iterations[k], [history of column c])."""
+    B = np.ascontiguousarray(B, np.float64)
+    n, k = B.shape
+    X = np.zeros_like(B) if X is None else np.array(X, dtype=np.float64, order="C")
+    its = np.zeros(k, np.int32)
+    hist = np.zeros(max(1, maxit) * k)
+    rc = lib().mgldg_pcg_batched(ctx.h, precon.h if precon is not None else None, A.h, k, B, X, tol, maxit, its,
+                                 hist)
+    ctx.check(rc, "pcg_batched")
+    hist = hist.reshape(k, max(1, maxit))
+    return X, its, [hist[c, :its[c]].copy() for c in range(k)]
+
+
+def batch_tiles(mg, level):
+    """Autotuned column tiles of a level: (spmm, jacobi, restrict, prolong, outer)."""
+    v = [C.c_int() for _ in range(5)]
+    rc = lib().mgldg_mg_batch_tiles(mg.h, level, *[C.byref(x) for x in v])
+    if rc:
+        raise MgldgError(rc, "batch_tiles")
+    return tuple(x.value for x in v)
 
 
 def _device_vectors(*arrays):
