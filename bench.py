@@ -210,6 +210,106 @@ def fp64_peak_tflops(torch):
     return 2 * n ** 3 / (best * 1e-3) / 1e12
 
 
+def run_batched(args, ctx, ext, torch, local, ws):
+    """Many right-hand sides: k seeded 8-Gaussian forcings (seeds 3001..)
+    solved together by the block PCG on a uniform Q2 mesh (the uniform
+    stand-in for the adaptive 2M-DOF quadtree of the multi-RHS workload),
+    mixed precision, damped block Jacobi (omega 0.7), V(2,2)."""
+    import mgldg
+    L = mgldg.lib()
+    k, nb, P = args.batched, args.batched_n, 3
+    levels = max(2, nb.bit_length() - 3)          # down to 4 x 4
+    prob = mgldg.CartesianProblem(ctx, P, nb, tau0=float(nb), tauD=float(nb))
+    ndof = prob.ndof
+    dev = f"cuda:{local}"
+    B = torch.empty((ndof, k), dtype=torch.float64, device=dev)
+    tmp = torch.empty(ndof, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    for c in range(k):
+        ctx.check(L.mgldg_problem_rhs_gaussian_dev(ctx.h, prob.h, 3001 + c, C.c_void_p(tmp.data_ptr())), "rhs")
+        ctx.sync()
+        B[:, c] = tmp
+    torch.cuda.synchronize()
+    X = torch.zeros_like(B)
+    mg = mgldg.Multigrid(ctx, prob.ops, prob.T, npre=2, npost=2, solver=mgldg.COARSE_DENSE, max_levels=levels,
+                         mean_project=0, relaxation=mgldg.RELAX_JACOBI, omega=0.7, precision=mgldg.PREC_MIXED)
+    A = prob.ops.A
+    its = np.zeros(k, np.int32)
+    hist = np.zeros(WL["maxit"] * k)
+
+    def solve():
+        with torch.cuda.stream(ext):
+            X.zero_()
+        ctx.check(L.mgldg_pcg_batched_dev(ctx.h, mg.h, A.h, k, C.c_void_p(B.data_ptr()), C.c_void_p(X.data_ptr()),
+                                          WL["tol"], WL["maxit"], its, hist), "pcg_batched")
+
+    t0 = time.perf_counter()
+    solve()                                       # first call: work space + tile autotuning
+    ctx.sync()
+    first_ms = (time.perf_counter() - t0) * 1e3
+    for _ in range(max(0, args.warmup - 1)):
+        solve()
+    ctx.sync()
+    dist_barrier(ws)
+    ctx.prof_reset()
+    steps = max(1, min(args.steps, 3))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    for _ in range(steps):
+        solve()
+    e1.record(ext)
+    e1.synchronize()
+    ms = dist_max(e0.elapsed_time(e1) / steps, ws)
+    launches = ctx.prof()
+    ctx.prof_enable(True)
+    ctx.prof_reset()
+    solve()
+    prof = ctx.prof()
+    ctx.prof_enable(False)
+    # single-RHS solve of column 0 with the same hierarchy for comparison
+    x1 = torch.zeros(ndof, dtype=torch.float64, device=dev)
+    b0 = B[:, 0].contiguous()
+    torch.cuda.synchronize()
+    it1 = C.c_int()
+    h1 = np.zeros(WL["maxit"])
+    for _ in range(2):
+        with torch.cuda.stream(ext):
+            x1.zero_()
+        ctx.check(L.mgldg_pcg_dev(ctx.h, mg.h, A.h, C.c_void_p(b0.data_ptr()), C.c_void_p(x1.data_ptr()),
+                                  WL["tol"], WL["maxit"], C.byref(it1), h1), "pcg")
+    ctx.sync()
+    e0.record(ext)
+    with torch.cuda.stream(ext):
+        x1.zero_()
+    ctx.check(L.mgldg_pcg_dev(ctx.h, mg.h, A.h, C.c_void_p(b0.data_ptr()), C.c_void_p(x1.data_ptr()),
+                              WL["tol"], WL["maxit"], C.byref(it1), h1), "pcg")
+    e1.record(ext)
+    e1.synchronize()
+    single_ms = e0.elapsed_time(e1)
+    torch.cuda.synchronize()
+    err0 = float(torch.linalg.norm(X[:, 0] - x1) / torch.linalg.norm(x1))
+    nbr, _, br, _, nnzb = A.info()
+    tiles = [mgldg.batch_tiles(mg, l) for l in range(mg.nlevels)]
+    out = {
+        "workload": (f"{nb}x{nb} uniform quadtree, Q2 LDG (9 DOF/element, {ndof:,} DOF), {k} right-hand sides "
+                     f"(seeds 3001..{3000 + k}), RATRAT {nb}->{nb >> (levels - 1)} ({levels} levels), mixed "
+                     f"precision, block Jacobi omega=0.7, V(2,2), tol 1e-10 per column"),
+        "k": k, "ms_per_batch": ms, "solves_per_s": k / (ms * 1e-3), "ms_per_rhs": ms / k,
+        "single_rhs_ms": single_ms, "batching_gain": single_ms / (ms / k),
+        "iters_min": int(its.min()), "iters_max": int(its.max()),
+        "col0_rel_diff_vs_single": err0,
+        "first_call_ms_incl_autotune": first_ms,
+        "tiles_level0": dict(zip(["spmm", "jacobi", "restrict", "prolong", "outer_fp64"], tiles[0])),
+        "kernel_ms": {kk: round(v[1], 3) for kk, v in prof.items() if v[0]},
+        "launches_per_batch": int(sum(v[0] for v in launches.values()) / steps),
+        "outer_fp64_spmm_gflop": 2 * nnzb * br * br * k / 1e9,
+        "steps": steps,
+    }
+    del B, X, tmp, mg, prob
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_gpu(args, ws, rank, local):
     import torch
     import mgldg
@@ -381,6 +481,11 @@ def run_gpu(args, ws, rank, local):
             e2e.append(dt * 1e3)
     e2e_ms = dist_max(float(np.mean(e2e)), ws)
 
+    batched = None
+    if args.batched > 0:
+        del mgs
+        batched = run_batched(args, ctx, ext, torch, local, ws)
+
     speedup = {}
     for sm in ("gs", "jacobi"):
         if f"fp64_{sm}" in results and f"mixed_{sm}" in results:
@@ -409,6 +514,7 @@ def run_gpu(args, ws, rank, local):
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 2 * ndof * 8, "d2h_bytes_per_step": ndof * 8,
                 "api": "mgldg_pcg (host buffers, pinned)"},
         "roofline": roof,
+        "batched": batched,
         "gpu_launches": gpu_launches,
         "clocks": clk,
     }
@@ -425,6 +531,8 @@ def main():
     ap.add_argument("--levels", type=int, default=WL["levels"])
     ap.add_argument("--forms", default="mixed_jacobi,fp64_jacobi,mixed_gs,fp64_gs")
     ap.add_argument("--headline", default="mixed_jacobi")
+    ap.add_argument("--batched", type=int, default=64, help="right-hand sides of the multi-RHS line (0: skip)")
+    ap.add_argument("--batched-n", type=int, default=512, help="mesh side of the multi-RHS line")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
