@@ -209,6 +209,50 @@ int mgldg_cartesian_h_interp(mgldg_ctx* ctx, int n_fine, int P, mgldg_bsr** T);
 int mgldg_cartesian_p_interp(mgldg_ctx* ctx, int ne, int P_fine, int P_coarse, mgldg_bsr** T);
 int mgldg_problem_rhs_gaussian_dev(mgldg_ctx* ctx, mgldg_problem* pr, uint64_t seed, double* b);
 
+/* ------------------------------------------------- adaptive quadtrees -- */
+/* Quadtree<2>(h) on [0,1]^2 (quadtree.tpp:10-40): a cell is split while its
+ * width exceeds h(centre).  balance != 0 adds 2:1 face balancing (no
+ * reference counterpart: a leaf is split while a face neighbour is two or
+ * more levels finer).  strategy: the coarsening of QuadTree::isLeaf
+ * (quadtree.h:164-173).  Host only, no GPU needed. */
+#define MGLDG_COARSEN_EQUAL 0
+#define MGLDG_COARSEN_RAPID 1
+typedef struct mgldg_quadtree mgldg_quadtree;
+typedef double (*mgldg_h_fn)(const double* x, void* user);
+int mgldg_quadtree_create(mgldg_h_fn h, void* user, int balance, int strategy, mgldg_quadtree** qt);
+int mgldg_quadtree_destroy(mgldg_quadtree* qt);
+int mgldg_quadtree_info(const mgldg_quadtree* qt, int* nnodes, int* nlevels, int* nleaves);
+/* Cells of layer l (QuadTree::layer, quadtree.h:176-186) in depth-first
+ * order as (level, ix, iy), cell = [ix, ix+1] x [iy, iy+1] * 2^-level.  With
+ * level, ix and iy all NULL only *n is returned. */
+int mgldg_quadtree_layer(const mgldg_quadtree* qt, int l, int* n, int* level, int* ix, int* iy);
+/* Built-in mesh-size rule (no reference counterpart; the adaptive mesh of
+ * the multi-RHS workload): a cell of width 2^-(base_level + l) is split while
+ * l < extra_levels and its centre lies within radius * 2^-l of one of the
+ * points, i.e. h(x) = min(2^-base, max(2^-(base+extra), d(x) / (radius 2^base)))
+ * with d the distance to the nearest point.  Pass mgldg_h_points with a
+ * mgldg_points_rule* as user. */
+typedef struct {
+    int npoints;
+    const double* points;   /* x0 y0 x1 y1 ... */
+    int base_level;
+    int extra_levels;
+    double radius;
+} mgldg_points_rule;
+double mgldg_h_points(const double* x, void* user);
+/* n seeded points in [0,1)^2: mt19937_64, 53-bit uniforms, (x, y) pairs. */
+int mgldg_seeded_points(uint64_t seed, int n, double* xy);
+/* LDG problem on the leaves of qt (Mesh(qt), mesh.h:186-264;
+ * LDGPoisson::discretize, ldgpoisson.tpp:27-100), homogeneous Dirichlet,
+ * with its h-interpolation hierarchy over the tree's layers
+ * (interpolationhierarchy.h:30-82).  tau_per_face != 0 (extension): interior
+ * penalty tau0 / min(h_L, h_R) and boundary penalty tauD / h_L instead of
+ * the constants tau0 and tauD. */
+int mgldg_quadtree_problem_create(mgldg_ctx* ctx, const mgldg_quadtree* qt, int P, double tau0,
+                                  double tauD, int tau_per_face, mgldg_problem** out);
+/* Faces, boundary faces and quadtree levels of a problem's mesh. */
+int mgldg_problem_mesh_info(const mgldg_problem* pr, int* nfaces, int* nbfaces, int* nlevels);
+
 /* ---------------------------------------------------------- file formats -- */
 /* Matrix Market dump of a BSR matrix, the format of the reference's
  * SparseBlockMatrix::write (sparseblockmatrix.tpp:145-164): coordinate real

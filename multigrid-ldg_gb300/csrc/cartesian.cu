@@ -20,21 +20,15 @@
 #include <random>
 
 #include "api.cuh"
-#include "master_tables.inc"
+#include "ldg_build.cuh"
 
 using namespace mg;
 
 namespace mg {
 
-typedef std::vector<double> Blk;   // row-major b x b
-
-struct Gauss8 {
-    double cx[8], cy[8], w[8], a[8];
-};
-
 // 8 Gaussians: centres U[0,1]^2, widths U[0.05,0.2], amplitudes N(0,1);
 // mt19937_64, 53-bit uniforms, Box-Muller with the cosine branch
-static Gauss8 gaussian_params(uint64_t seed) {
+Gauss8 gaussian_params(uint64_t seed) {
     std::mt19937_64 g(seed);
     auto uni = [&]() { return (double)(g() >> 11) * 0x1.0p-53; };
     Gauss8 p;
@@ -66,94 +60,6 @@ static void morton_decode(uint32_t e, uint32_t& ix, uint32_t& iy) {
     }
 }
 
-struct Ref2 {
-    int P, b;
-    const double* nodes;
-    const double* denom;
-    const double* mass1;
-    const double* invmass1;
-    const double* diff1;
-    explicit Ref2(int P_) : P(P_), b(P_ * P_) {
-        nodes = kNodes[P - 1]; denom = kDenom[P - 1];
-        mass1 = kMass1[P - 1]; invmass1 = kInvMass1[P - 1]; diff1 = kDiff1[P - 1];
-    }
-    // tensorProduct<2,P> (master.h:121-135)
-    Blk tensor(const double* A) const {
-        Blk M((size_t)b * b);
-        for (int i0 = 0; i0 < P; ++i0)
-            for (int i1 = 0; i1 < P; ++i1)
-                for (int j0 = 0; j0 < P; ++j0)
-                    for (int j1 = 0; j1 < P; ++j1) {
-                        double v = 1.0;
-                        v *= A[i0 * P + j0];
-                        v *= A[i1 * P + j1];
-                        M[(size_t)(i0 * P + i1) * b + j0 * P + j1] = v;
-                    }
-        return M;
-    }
-    // Master<2,P>::diff(dim) (master.h:45-68)
-    Blk diff(int dim) const {
-        Blk D((size_t)b * b, 0.0);
-        for (int i0 = 0; i0 < P; ++i0)
-            for (int i1 = 0; i1 < P; ++i1)
-                for (int j0 = 0; j0 < P; ++j0)
-                    for (int j1 = 0; j1 < P; ++j1) {
-                        int it[2] = {i0, i1}, jt[2] = {j0, j1};
-                        if (it[1 - dim] != jt[1 - dim]) continue;
-                        D[(size_t)(i0 * P + i1) * b + j0 * P + j1] = diff1[it[dim] * P + jt[dim]];
-                    }
-        return D;
-    }
-    // LagrangePoly<P>::eval (master.h:79-94)
-    void lagrange1(double x, double* l) const {
-        double alpha = 1;
-        l[0] = denom[0];
-        for (int i = 0; i < P - 1; ++i) {
-            alpha *= x - nodes[i];
-            l[i + 1] = alpha * denom[i + 1];
-        }
-        double beta = 1;
-        for (int i = P - 1; i > 0; --i) {
-            beta *= x - nodes[i];
-            l[i - 1] *= beta;
-        }
-    }
-    void lagrange2(const double* x, double* out) const {
-        double g0[8], g1[8];
-        lagrange1(x[0], g0);
-        lagrange1(x[1], g1);
-        for (int i0 = 0; i0 < P; ++i0)
-            for (int i1 = 0; i1 < P; ++i1) {
-                double v = 1;
-                v *= g0[i0];
-                v *= g1[i1];
-                out[i0 * P + i1] = v;
-            }
-    }
-};
-
-static Blk bscale(double s, const Blk& A) {
-    Blk C(A.size());
-    for (size_t k = 0; k < A.size(); ++k) C[k] = s * A[k];
-    return C;
-}
-static Blk bmul(const Blk& A, const Blk& B, int b) {
-    Blk C((size_t)b * b);
-    for (int i = 0; i < b; ++i)
-        for (int j = 0; j < b; ++j) {
-            double s = 0;
-            for (int k = 0; k < b; ++k) s += A[(size_t)i * b + k] * B[(size_t)k * b + j];
-            C[(size_t)i * b + j] = s;
-        }
-    return C;
-}
-static Blk btrans(const Blk& A, int b) {
-    Blk C(A.size());
-    for (int i = 0; i < b; ++i)
-        for (int j = 0; j < b; ++j) C[(size_t)j * b + i] = A[(size_t)i * b + j];
-    return C;
-}
-
 // out block o = sum of table[tidx[t]], t in [tptr[o], tptr[o+1]) in order
 __global__ void k_sum_blocks(int64_t nout, int bsz, const int64_t* __restrict__ tptr, const int* __restrict__ tidx,
                              const double* __restrict__ table, double* __restrict__ out) {
@@ -169,20 +75,18 @@ __global__ void k_sum_blocks(int64_t nout, int bsz, const int64_t* __restrict__ 
 }
 
 // b_e = M_e f_e with f the Gaussian sum at the element's Gauss-Lobatto nodes
+// and M_e = |e| M_ref (Element::mass, mesh.h:143-147)
 struct GaussDev {
     double cx[8], cy[8], w[8], a[8];
 };
-__global__ void k_rhs_gaussian(int ne, int P, int n, double h, GaussDev g, const double* __restrict__ nodes,
-                               const double* __restrict__ Mblk, double* __restrict__ out) {
+__global__ void k_rhs_gaussian(int ne, int P, const double* __restrict__ geom, GaussDev g,
+                               const double* __restrict__ nodes, const double* __restrict__ Mref,
+                               double* __restrict__ out) {
     extern __shared__ double sf[];
     const int b = P * P;
     for (int e = blockIdx.x; e < ne; e += gridDim.x) {
-        uint32_t ix = 0, iy = 0;
-        for (int bit = 0; bit < 16; ++bit) {
-            ix |= (((uint32_t)e >> (2 * bit + 1)) & 1u) << bit;
-            iy |= (((uint32_t)e >> (2 * bit)) & 1u) << bit;
-        }
-        const double lox = ix * h, loy = iy * h;
+        const double lox = geom[e], loy = geom[ne + e], h = geom[2 * ne + e];
+        const double vol = h * h;
         for (int q = threadIdx.x; q < b; q += blockDim.x) {
             const int i0 = q / P, i1 = q - i0 * P;
             const double x = lox + h * nodes[i0], y = loy + h * nodes[i1];
@@ -196,7 +100,7 @@ __global__ void k_rhs_gaussian(int ne, int P, int n, double h, GaussDev g, const
         __syncthreads();
         for (int r = threadIdx.x; r < b; r += blockDim.x) {
             double s = 0;
-            for (int c = 0; c < b; ++c) s += Mblk[r * b + c] * sf[c];
+            for (int c = 0; c < b; ++c) s += (vol * Mref[r * b + c]) * sf[c];
             out[(size_t)e * b + r] = s;
         }
         __syncthreads();
@@ -205,43 +109,9 @@ __global__ void k_rhs_gaussian(int ne, int P, int n, double h, GaussDev g, const
 
 }  // namespace mg
 
-struct mgldg_problem {
-    mgldg_ctx* ctx = nullptr;
-    int P = 0, b = 0, n = 0, ne = 0;
-    double h = 0;
-    mgldg_ops* ops = nullptr;
-    std::vector<mgldg_bsr*> T;
-    double* d_nodes = nullptr;
-    double* d_M = nullptr;
-    ~mgldg_problem() {
-        delete ops;
-        for (auto* t : T) delete t;
-        dfree(d_nodes);
-        dfree(d_M);
-    }
-};
-
 namespace mg {
 
-// builds one operator from per-block contribution lists
-struct Assembly {
-    std::vector<int> row_ptr, col_idx;
-    std::vector<int64_t> tptr{0};
-    std::vector<int> tidx;
-    void begin_row() {}
-    void add_block(int col, std::initializer_list<int> contrib) {
-        col_idx.push_back(col);
-        for (int c : contrib) tidx.push_back(c);
-        tptr.push_back((int64_t)tidx.size());
-    }
-    void add_block_v(int col, const std::vector<int>& contrib) {
-        col_idx.push_back(col);
-        for (int c : contrib) tidx.push_back(c);
-        tptr.push_back((int64_t)tidx.size());
-    }
-};
-
-static mgldg_bsr* realize(mgldg_ctx* ctx, const Assembly& As, int ne, int b, const double* d_table) {
+mgldg_bsr* realize(mgldg_ctx* ctx, const Assembly& As, int ne, int b, const double* d_table) {
     mgldg_bsr* A = bsr_new(ctx, ne, ne, b, b, As.row_ptr, As.col_idx);
     int64_t* dptr = nullptr;
     int* didx = nullptr;
@@ -272,7 +142,7 @@ static mgldg_bsr* realize(mgldg_ctx* ctx, const Assembly& As, int ne, int b, con
 
 // A block-CSR operator with one block per row, given column per row and a
 // table of distinct blocks (br x bc) indexed per row.
-static mgldg_bsr* table_operator(mgldg_ctx* ctx, int nbr, int nbc, int br, int bc, const std::vector<int>& col,
+mgldg_bsr* table_operator(mgldg_ctx* ctx, int nbr, int nbc, int br, int bc, const std::vector<int>& col,
                                  const std::vector<int>& blk, const std::vector<double>& table) {
     mgldg_bsr* T = new mgldg_bsr();
     try {
@@ -502,10 +372,20 @@ static mgldg_problem* cartesian_create(mgldg_ctx* ctx, int P, int n, double tau0
         pr->ops->G[1] = G1; G1 = nullptr;
         pr->ops->T = Tm; Tm = nullptr;
         construct_laplacian(ctx, pr->ops);
-        pr->d_nodes = dalloc<double>(P);
-        upload(ctx, pr->d_nodes, R.nodes, P);
-        pr->d_M = dalloc<double>((size_t)b * b);
-        upload(ctx, pr->d_M, Mblk.data(), Mblk.size());
+        pr->ex.resize(ne);
+        pr->ey.resize(ne);
+        pr->ew.assign(ne, h);
+        for (int e = 0; e < ne; ++e) {
+            uint32_t ix, iy;
+            morton_decode((uint32_t)e, ix, iy);
+            pr->ex[e] = ix * h;
+            pr->ey[e] = iy * h;
+        }
+        pr->nlevels = 1;
+        for (int m = n; m > 1; m >>= 1) ++pr->nlevels;
+        pr->nbfaces = 4 * n;
+        pr->nfaces = 2 * n * (n - 1) + pr->nbfaces;
+        problem_upload_geometry(ctx, pr);
 
         // ---- h-interpolation hierarchy (interpolationhierarchy.h:30-82) ----
         for (int nf = n; nf > 1; nf >>= 1) pr->T.push_back(h_interp(ctx, nf, P));
@@ -527,11 +407,11 @@ static void rhs_gaussian_dev(mgldg_ctx* ctx, mgldg_problem* pr, uint64_t seed, d
     std::memcpy(gd.cy, g.cy, sizeof g.cy);
     std::memcpy(gd.w, g.w, sizeof g.w);
     std::memcpy(gd.a, g.a, sizeof g.a);
-    int grid = std::min(pr->ne, ctx->sm_count * 32);
+    int grid = std::max(1, std::min(pr->ne, ctx->sm_count * 32));
     {
         Launch L(ctx, MGLDG_K_SETUP);
-        k_rhs_gaussian<<<grid, 128, pr->b * sizeof(double), ctx->stream>>>(pr->ne, pr->P, pr->n, pr->h, gd, pr->d_nodes,
-                                                                           pr->d_M, b);
+        k_rhs_gaussian<<<grid, 128, pr->b * sizeof(double), ctx->stream>>>(pr->ne, pr->P, pr->d_geom, gd,
+                                                                           pr->d_nodes, pr->d_Mref, b);
     }
     check_launch();
 }
@@ -555,9 +435,29 @@ extern "C" int mgldg_problem_destroy(mgldg_problem* pr) {
 }
 
 namespace mg {
-void problem_geometry(const mgldg_problem* pr, int* P, int* n) {
+void problem_boxes(const mgldg_problem* pr, int* P, int* ne, const double** ex, const double** ey,
+                   const double** ew) {
     *P = pr->P;
-    *n = pr->n;
+    *ne = pr->ne;
+    *ex = pr->ex.data();
+    *ey = pr->ey.data();
+    *ew = pr->ew.data();
+}
+
+void problem_upload_geometry(mgldg_ctx* ctx, mgldg_problem* pr) {
+    const Ref2 R(pr->P);
+    const int ne = pr->ne, b = pr->b;
+    std::vector<double> g((size_t)3 * ne);
+    std::copy(pr->ex.begin(), pr->ex.end(), g.begin());
+    std::copy(pr->ey.begin(), pr->ey.end(), g.begin() + ne);
+    std::copy(pr->ew.begin(), pr->ew.end(), g.begin() + 2 * (size_t)ne);
+    pr->d_geom = dalloc<double>(std::max<size_t>(1, g.size()));
+    upload(ctx, pr->d_geom, g.data(), g.size());
+    pr->d_nodes = dalloc<double>(pr->P);
+    upload(ctx, pr->d_nodes, R.nodes, pr->P);
+    const Blk Mref = R.tensor(R.mass1);
+    pr->d_Mref = dalloc<double>((size_t)b * b);
+    upload(ctx, pr->d_Mref, Mref.data(), Mref.size());
 }
 }  // namespace mg
 

@@ -97,27 +97,23 @@ extern "C" int mgldg_bsr_read_mtx(mgldg_ctx* ctx, const char* path, int br, int 
 
 struct mgldg_problem;
 namespace mg {
-// geometry of the uniform Cartesian problem (defined in cartesian.cu)
-void problem_geometry(const mgldg_problem* pr, int* P, int* n);
+// element boxes of a problem (defined in cartesian.cu)
+void problem_boxes(const mgldg_problem* pr, int* P, int* ne, const double** ex, const double** ey,
+                   const double** ew);
 }
 
 extern "C" int mgldg_problem_write_fun(mgldg_ctx* ctx, const mgldg_problem* pr, const double* u, const char* path) {
     MG_API_BEGIN(ctx)
     MG_REQUIRE(pr && u && path, MGLDG_ERR_ARG, "null argument");
-    int P = 0, n = 0;
-    problem_geometry(pr, &P, &n);
-    const double h = 1.0 / n;
-    const int ne = n * n, b = P * P;
+    int P = 0, ne = 0;
+    const double *ex = nullptr, *ey = nullptr, *ew = nullptr;
+    problem_boxes(pr, &P, &ne, &ex, &ey, &ew);
+    const int b = P * P;
     FILE* f = std::fopen(path, "w");
     MG_REQUIRE(f != nullptr, MGLDG_ERR_ARG, std::string("cannot open ") + path);
     std::fprintf(f, "%d %d %d\n", P, 2, ne);
     for (int e = 0; e < ne; ++e) {
-        uint32_t ix = 0, iy = 0;
-        for (int bit = 0; bit < 16; ++bit) {
-            ix |= (((uint32_t)e >> (2 * bit + 1)) & 1u) << bit;
-            iy |= (((uint32_t)e >> (2 * bit)) & 1u) << bit;
-        }
-        const double lo[2] = {ix * h, iy * h};
+        const double lo[2] = {ex[e], ey[e]}, h = ew[e];
         for (int i0 = 0; i0 < P; ++i0)
             for (int i1 = 0; i1 < P; ++i1) {
                 const double x = lo[0] + h * kNodes[P - 1][i0], y = lo[1] + h * kNodes[P - 1][i1];

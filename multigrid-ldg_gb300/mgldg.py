@@ -39,7 +39,9 @@ EXPORTS = [
     "mgldg_bsr_write_mtx", "mgldg_bsr_read_mtx", "mgldg_problem_write_fun",
     "mgldg_ops_construct_laplacian_kappa", "mgldg_kappa_gradient_dev", "mgldg_adjoint_l2_dev",
     "mgldg_bsr_mm_dev", "mgldg_mg_vcycle_batched_dev", "mgldg_pcg_batched_dev", "mgldg_pcg_batched",
-    "mgldg_mg_batch_tiles",
+    "mgldg_mg_batch_tiles", "mgldg_quadtree_create", "mgldg_quadtree_destroy", "mgldg_quadtree_info",
+    "mgldg_quadtree_layer", "mgldg_h_points", "mgldg_seeded_points", "mgldg_quadtree_problem_create",
+    "mgldg_problem_mesh_info",
 ]
 
 
@@ -146,6 +148,15 @@ def lib():
         L.mgldg_pcg_batched_dev.argtypes = [vp, vp, vp, C.c_int, vp, vp, C.c_double, C.c_int, _ip, _dp]
         L.mgldg_pcg_batched.argtypes = [vp, vp, vp, C.c_int, _dp, _dp, C.c_double, C.c_int, _ip, _dp]
         L.mgldg_mg_batch_tiles.argtypes = [vp, C.c_int, ip, ip, ip, ip, ip]
+        L.mgldg_quadtree_create.argtypes = [vp, vp, C.c_int, C.c_int, pvp]
+        L.mgldg_quadtree_destroy.argtypes = [vp]
+        L.mgldg_quadtree_info.argtypes = [vp, ip, ip, ip]
+        L.mgldg_quadtree_layer.argtypes = [vp, C.c_int, ip, vp, vp, vp]
+        L.mgldg_h_points.argtypes = [C.POINTER(C.c_double), vp]
+        L.mgldg_h_points.restype = C.c_double
+        L.mgldg_seeded_points.argtypes = [C.c_uint64, C.c_int, _dp]
+        L.mgldg_quadtree_problem_create.argtypes = [vp, vp, C.c_int, C.c_double, C.c_double, C.c_int, pvp]
+        L.mgldg_problem_mesh_info.argtypes = [vp, ip, ip, ip]
         _lib = L
     return _lib
 
@@ -481,15 +492,89 @@ def hp_chain(ctx, n, degrees, nh):
     return T
 
 
-class CartesianProblem:
-    """Uniform n x n quadtree mesh, Q_{P-1} LDG operators and hierarchy, built on the GPU."""
+COARSEN_EQUAL, COARSEN_RAPID = 0, 1
+H_FN = C.CFUNCTYPE(C.c_double, C.POINTER(C.c_double), C.c_void_p)
 
-    def __init__(self, ctx, P, n, tau0=None, tauD=None):
-        tau0 = float(n) if tau0 is None else tau0
-        tauD = float(n) if tauD is None else tauD
+
+class PointsRule(C.Structure):
+    _fields_ = [("npoints", C.c_int), ("points", C.POINTER(C.c_double)), ("base_level", C.c_int),
+                ("extra_levels", C.c_int), ("radius", C.c_double)]
+
+
+def seeded_points(seed, n):
+    """n points in [0,1)^2 from mt19937_64 (53-bit uniforms, x/y pairs)."""
+    xy = np.zeros(2 * n)
+    rc = lib().mgldg_seeded_points(seed, n, xy)
+    if rc:
+        raise MgldgError(rc, "seeded_points")
+    return xy.reshape(n, 2)
+
+
+class Quadtree:
+    """Quadtree<2>(h) on [0,1]^2 (host): h is a Python callable h(x, y) -> width,
+    or use Quadtree.points(...) for the built-in seeded-points rule."""
+
+    def __init__(self, h=None, balance=False, strategy=COARSEN_EQUAL, _native=None):
+        out = C.c_void_p()
+        if _native is not None:
+            fn, user = _native
+        else:
+            self._cb = H_FN(lambda x, _u: float(h(x[0], x[1])))
+            fn, user = C.cast(self._cb, C.c_void_p), None
+        rc = lib().mgldg_quadtree_create(fn, user, int(balance), strategy, C.byref(out))
+        if rc:
+            raise MgldgError(rc, "quadtree_create")
+        self.h = out
+        a, b_, c = C.c_int(), C.c_int(), C.c_int()
+        lib().mgldg_quadtree_info(out, C.byref(a), C.byref(b_), C.byref(c))
+        self.nnodes, self.nlevels, self.nleaves = a.value, b_.value, c.value
+
+    @classmethod
+    def points(cls, points, base_level, extra_levels, radius=0.5, balance=True, strategy=COARSEN_EQUAL):
+        pts = np.ascontiguousarray(points, np.float64).ravel()
+        rule = PointsRule(len(pts) // 2, pts.ctypes.data_as(C.POINTER(C.c_double)), base_level, extra_levels, radius)
+        fn = C.cast(lib().mgldg_h_points, C.c_void_p)
+        self = cls(balance=balance, strategy=strategy, _native=(fn, C.cast(C.pointer(rule), C.c_void_p)))
+        return self
+
+    def layer(self, l):
+        n = C.c_int()
+        rc = lib().mgldg_quadtree_layer(self.h, l, C.byref(n), None, None, None)
+        if rc:
+            raise MgldgError(rc, "quadtree_layer")
+        lev, ix, iy = (np.zeros(n.value, np.int32) for _ in range(3))
+        p = lambda a: a.ctypes.data_as(C.c_void_p)
+        lib().mgldg_quadtree_layer(self.h, l, C.byref(n), p(lev), p(ix), p(iy))
+        return lev, ix, iy
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            try:
+                lib().mgldg_quadtree_destroy(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+
+class CartesianProblem:
+    """Uniform n x n quadtree mesh, Q_{P-1} LDG operators and hierarchy, built on the GPU
+    (or, with quadtree=..., the leaves of an adaptive Quadtree)."""
+
+    def __init__(self, ctx, P, n=None, tau0=None, tauD=None, quadtree=None, tau_per_face=False):
         h = C.c_void_p()
-        ctx.check(lib().mgldg_cartesian_create(ctx.h, P, n, tau0, tauD, C.byref(h)), "cartesian_create")
+        if quadtree is None:
+            tau0 = float(n) if tau0 is None else tau0
+            tauD = float(n) if tauD is None else tauD
+            ctx.check(lib().mgldg_cartesian_create(ctx.h, P, n, tau0, tauD, C.byref(h)), "cartesian_create")
+        else:
+            tau0 = 1.0 if tau0 is None else tau0
+            tauD = 1.0 if tauD is None else tauD
+            ctx.check(lib().mgldg_quadtree_problem_create(ctx.h, quadtree.h, P, tau0, tauD, int(tau_per_face),
+                                                          C.byref(h)), "quadtree_problem_create")
         self.ctx, self.h = ctx, h
+        nf, nb, nl = C.c_int(), C.c_int(), C.c_int()
+        lib().mgldg_problem_mesh_info(h, C.byref(nf), C.byref(nb), C.byref(nl))
+        self.nfaces, self.nbfaces, self.nlevels = nf.value, nb.value, nl.value
         ne, npl, nT = C.c_int(), C.c_int(), C.c_int()
         ndof = C.c_int64()
         ctx.check(lib().mgldg_problem_info(h, C.byref(ne), C.byref(npl), C.byref(ndof), C.byref(nT)), "info")

@@ -567,6 +567,57 @@ struct Quadtree {
             tree[id].height++;
         }
     }
+    // Extension (the reference does not balance its trees): 2:1 face
+    // balance.  A leaf is split while a face neighbour leaf is two or more
+    // levels finer; only forced splits are made, so the result is the
+    // unique coarsest balanced refinement.
+    void split(int id) {
+        double mid[2];
+        for (int i = 0; i < NDIM; ++i) mid[i] = tree[id].cell.lo[i] + tree[id].cell.width(i) / 2;
+        for (int b0 = 0; b0 < 2; ++b0)
+            for (int b1 = 0; b1 < 2; ++b1) {
+                int bits[2] = {b0, b1};
+                Cell c = tree[id].cell;
+                for (int i = 0; i < NDIM; ++i) {
+                    if (bits[i]) c.lo[i] = mid[i];
+                    else c.hi[i] = mid[i];
+                }
+                Node nd;
+                nd.id = (int)tree.size(); nd.parent = id; nd.cell = c;
+                nd.level = tree[id].level + 1;
+                tree.push_back(nd);
+                tree[id].children[b0 * 2 + b1] = nd.id;
+            }
+        numLevels = std::max(numLevels, tree[id].level + 2);
+        for (int a = id; a >= 0; a = tree[a].parent) {
+            int h = 0;
+            for (int k = 0; k < 4; ++k) h = std::max(h, tree[tree[a].children[k]].height + 1);
+            if (tree[a].height == h && a != id) break;
+            tree[a].height = h;
+        }
+    }
+    void balance() {
+        bool changed = true;
+        while (changed) {
+            changed = false;
+            std::vector<int> leaves;
+            for (const Node& nd : tree)
+                if (nd.children[0] < 0) leaves.push_back(nd.id);
+            for (int id : leaves) {
+                bool need = false;
+                for (int i = 0; i < NDIM && !need; ++i)
+                    for (Direction dir : {kLeft, kRight}) {
+                        for (int nb : neighbors(id, i, dir, 0))
+                            if (tree[nb].level >= tree[id].level + 2) need = true;
+                        if (need) break;
+                    }
+                if (need) {
+                    split(id);
+                    changed = true;
+                }
+            }
+        }
+    }
     // quadtree.h:164-173
     bool isLeaf(const Node& node, int coarsening) const {
         if (strategy == ORC_COARSEN_RAPID) {
@@ -854,6 +905,7 @@ struct Problem {
     int bctype;
     std::function<double(const double*)> bcfun;   // boundary value
     double tau0, tauD;
+    bool tau_per_face = false;   // extension: tau0 / min(h_L, h_R), tauD / h_L
     std::vector<double> rhs, utrue;
     std::vector<std::vector<Mat>> Tl;   // unused placeholder
     std::vector<SBM> hier;             // InterpolationHierarchy<2,P>::T
@@ -894,14 +946,18 @@ static void discretize(Problem& pr, std::vector<double>& rhs) {
             Mat MinvR = mesh.invmass(f.right);
             ops.G[f.dim].add(f.right, f.right, matmul(scaled(n, MinvR), RR));
             ops.G[f.dim].add(f.right, f.left, matmul(scaled(-n, MinvR), RL));
-            ops.T.add(f.right, f.right, scaled(pr.tau0, RR));
-            ops.T.add(f.left, f.left, scaled(pr.tau0, LL));
-            ops.T.add(f.right, f.left, scaled(-pr.tau0, RL));
-            ops.T.add(f.left, f.right, scaled(-pr.tau0, transpose(RL)));
+            double tau = pr.tau0;
+            if (pr.tau_per_face)
+                tau = pr.tau0 / std::min(mesh.elements[f.left].width(0), mesh.elements[f.right].width(0));
+            ops.T.add(f.right, f.right, scaled(tau, RR));
+            ops.T.add(f.left, f.left, scaled(tau, LL));
+            ops.T.add(f.right, f.left, scaled(-tau, RL));
+            ops.T.add(f.left, f.right, scaled(-tau, transpose(RL)));
         } else if (pr.bctype == kDirichlet) {
             Mat MinvL = mesh.invmass(f.left);
             ops.G[f.dim].add(f.left, f.left, matmul(scaled(-n, MinvL), LL));
-            ops.T.add(f.left, f.left, scaled(pr.tauD, LL));
+            double tauD = pr.tau_per_face ? pr.tauD / mesh.elements[f.left].width(0) : pr.tauD;
+            ops.T.add(f.left, f.left, scaled(tauD, LL));
         }
     }
     ops.construct_laplacian();
@@ -930,7 +986,8 @@ static void discretize(Problem& pr, std::vector<double>& rhs) {
         if (pr.bctype == kDirichlet) {
             for (int a = 0; a < npl; ++a) {
                 Jg[f.dim][(size_t)npl * f.left + a] += n * Lbc[a];
-                rhs[(size_t)npl * f.left + a] += pr.tauD * Lbc[a];
+                rhs[(size_t)npl * f.left + a] +=
+                    (pr.tau_per_face ? pr.tauD / mesh.elements[f.left].width(0) : pr.tauD) * Lbc[a];
             }
         } else if (pr.bctype == kNeumann) {
             for (int a = 0; a < npl; ++a) rhs[(size_t)npl * f.left + a] += Lbc[a];
@@ -1059,10 +1116,12 @@ static std::vector<double> interpolate(const Mesh& mesh, const std::function<dou
     return v;
 }
 
+static Problem* problem_create_h(int P, const std::function<double(const double*)>& h, int balance,
+                                 int tau_per_face, int coarsening, int bctype, int test, double tau0,
+                                 double tauD, uint64_t seed);
+
 static Problem* problem_create(int P, double dx, int refine, int coarsening, int bctype, int test,
                                double tau0, double tauD, uint64_t seed) {
-    std::unique_ptr<Problem> pr(new Problem());
-    pr->P = P; pr->npl = P * P; pr->bctype = bctype; pr->tau0 = tau0; pr->tauD = tauD;
     std::function<double(const double*)> h;
     if (refine == ORC_REFINE_UNIFORM) {
         h = [dx](const double*) { return dx; };
@@ -1070,7 +1129,39 @@ static Problem* problem_create(int P, double dx, int refine, int coarsening, int
         // h_adaptive (dg_tests.cpp:212-215)
         h = [dx](const double* x) { return (x[0] > 0.5) ? dx : (x[0] > 0.25) ? 0.25 * dx : 0.5 * dx; };
     }
+    return problem_create_h(P, h, 0, 0, coarsening, bctype, test, tau0, tauD, seed);
+}
+
+// Seeded points: mt19937_64 with 53-bit uniforms, (x, y) pairs.
+static std::vector<double> seeded_points(uint64_t seed, int n) {
+    std::mt19937_64 g(seed);
+    std::vector<double> p(2 * (size_t)n);
+    for (auto& v : p) v = (double)(g() >> 11) * 0x1.0p-53;
+    return p;
+}
+
+// Mesh size of the seeded-points refinement: a cell of width
+// w = 2^-(base + l) is split while l < extra and its centre lies within
+// radius * 2^-l of a point; as an h(x) callback (split iff w > h(centre)):
+// h = min(2^-base, max(2^-(base+extra), d / (radius 2^base))).
+static double points_h(const std::vector<double>& pts, int base, int extra, double radius, const double* x) {
+    double d = 1e300;
+    for (size_t k = 0; k + 1 < pts.size(); k += 2) {
+        const double dx = x[0] - pts[k], dy = x[1] - pts[k + 1];
+        d = std::min(d, std::sqrt(dx * dx + dy * dy));
+    }
+    const double lo = std::ldexp(1.0, -(base + extra)), hi = std::ldexp(1.0, -base);
+    return std::min(hi, std::max(lo, d / (radius * std::ldexp(1.0, base))));
+}
+
+static Problem* problem_create_h(int P, const std::function<double(const double*)>& h, int balance,
+                                 int tau_per_face, int coarsening, int bctype, int test, double tau0,
+                                 double tauD, uint64_t seed) {
+    std::unique_ptr<Problem> pr(new Problem());
+    pr->P = P; pr->npl = P * P; pr->bctype = bctype; pr->tau0 = tau0; pr->tauD = tauD;
+    pr->tau_per_face = tau_per_face != 0;
     pr->qt.reset(new Quadtree(h, coarsening, bctype == kPeriodic));
+    if (balance) pr->qt->balance();
     pr->mesh.reset(new Mesh(*pr->qt, P));
     pr->ops = std::make_shared<Ops>();
     const double PI = 3.14159265358979323846;
@@ -1447,6 +1538,26 @@ int orc_problem_create(int P, double dx, int refine, int coarsening, int bctype,
                        double tau0, double tauD, uint64_t seed, orc_problem** out) {
     ORC_TRY({
         *out = new orc_problem{problem_create(P, dx, refine, coarsening, bctype, test, tau0, tauD, seed)};
+    })
+}
+int orc_problem_create_points(int P, int base_level, int extra_levels, int npoints, uint64_t point_seed,
+                              double radius, int balance, int tau_per_face, double tau0, double tauD,
+                              uint64_t rhs_seed, orc_problem** out) {
+    ORC_TRY({
+        if (base_level < 0 || extra_levels < 0 || base_level + extra_levels > 20 || npoints < 1 || !(radius > 0))
+            throw std::invalid_argument("bad points rule");
+        std::vector<double> pts = seeded_points(point_seed, npoints);
+        std::function<double(const double*)> h = [pts, base_level, extra_levels, radius](const double* x) {
+            return points_h(pts, base_level, extra_levels, radius, x);
+        };
+        *out = new orc_problem{problem_create_h(P, h, balance, tau_per_face, ORC_COARSEN_EQUAL, kDirichlet,
+                                                ORC_TEST_GAUSSIAN, tau0, tauD, rhs_seed)};
+    })
+}
+int orc_seeded_points(uint64_t seed, int n, double* xy) {
+    ORC_TRY({
+        std::vector<double> p = seeded_points(seed, n);
+        std::copy(p.begin(), p.end(), xy);
     })
 }
 int orc_problem_destroy(orc_problem* pr) {

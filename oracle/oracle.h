@@ -58,6 +58,16 @@ enum { ORC_COARSEN_EQUAL = 0, ORC_COARSEN_RAPID = 1 };
 int orc_problem_create(int P, double dx, int refine, int coarsening, int bctype,
                        int test, double tau0, double tauD, uint64_t seed,
                        orc_problem** out);
+/* Adaptive quadtree of the seeded-points rule (extension; the multi-RHS
+ * workload's mesh): a cell of width 2^-(base+l) is split while l < extra and
+ * its centre lies within radius*2^-l of one of npoints seeded points
+ * (mt19937_64, 53-bit uniforms, x/y pairs), optionally 2:1 face balanced;
+ * tau_per_face: penalties tau0/min(h_L,h_R) and tauD/h_L instead of the
+ * reference's constants.  Homogeneous Dirichlet, Gaussian-sum rhs. */
+int orc_problem_create_points(int P, int base_level, int extra_levels, int npoints, uint64_t point_seed,
+                              double radius, int balance, int tau_per_face, double tau0, double tauD,
+                              uint64_t rhs_seed, orc_problem** out);
+int orc_seeded_points(uint64_t seed, int n, double* xy);
 int orc_problem_destroy(orc_problem* pr);
 /* ne, npl (=P^2), number of DOFs, number of quadtree levels, faces, boundary faces */
 int orc_problem_info(const orc_problem* pr, int* ne, int* npl, int* ndof,

@@ -79,6 +79,9 @@ def lib():
         L.orc_problem_mv.argtypes = [vp, C.c_int, C.c_double, _dp, C.c_double, _dp]
         L.orc_problem_write_mtx.argtypes = [vp, C.c_int, C.c_char_p]
         L.orc_problem_write_fun.argtypes = [vp, _dp, C.c_char_p]
+        L.orc_problem_create_points.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_double,
+                                                C.c_int, C.c_int, C.c_double, C.c_double, C.c_uint64, pvp]
+        L.orc_seeded_points.argtypes = [C.c_uint64, C.c_int, _dp]
         _lib = L
     return _lib
 
@@ -100,6 +103,12 @@ def quadrature(Q):
     x, w = np.zeros(Q), np.zeros(Q)
     _ck(lib().orc_quadrature(Q, x, w), "quadrature")
     return x, w
+
+
+def seeded_points(seed, n):
+    xy = np.zeros(2 * n)
+    _ck(lib().orc_seeded_points(seed, n, xy), "seeded_points")
+    return xy.reshape(n, 2)
 
 
 def gaussian_params(seed):
@@ -178,6 +187,20 @@ class Problem:
         h = C.c_void_p()
         _ck(lib().orc_problem_create(P, dx, refine, coarsening, bc, test, tau0, tauD, seed,
                                      C.byref(h)), "problem_create")
+        self._attach(h, P)
+
+    @classmethod
+    def points(cls, P, base_level, extra_levels, npoints=4, point_seed=3000, radius=0.5, balance=True,
+               tau_per_face=True, tau0=1.0, tauD=1.0, seed=3001):
+        """Adaptive quadtree of the seeded-points rule (see oracle.h)."""
+        self = cls.__new__(cls)
+        h = C.c_void_p()
+        _ck(lib().orc_problem_create_points(P, base_level, extra_levels, npoints, point_seed, radius, int(balance),
+                                            int(tau_per_face), tau0, tauD, seed, C.byref(h)), "create_points")
+        self._attach(h, P)
+        return self
+
+    def _attach(self, h, P):
         self.h = h
         vals = [C.c_int() for _ in range(6)]
         _ck(lib().orc_problem_info(h, *[C.byref(v) for v in vals]), "info")
