@@ -253,6 +253,36 @@ int mgldg_quadtree_problem_create(mgldg_ctx* ctx, const mgldg_quadtree* qt, int 
 /* Faces, boundary faces and quadtree levels of a problem's mesh. */
 int mgldg_problem_mesh_info(const mgldg_problem* pr, int* nfaces, int* nbfaces, int* nlevels);
 
+/* ---------------------------------------------- unstructured triangles -- */
+/* Mesh input.  mgldg_mesh_read reads the reference's .mesh wireframe
+ * (Wireframe(file), wireframe.h:24-67): "np nt", a header line, np lines of
+ * x y, an empty line, nt lines of 1-based vertex triples; p[2*np], t[3*nt]
+ * 0-based (pass p = t = NULL to get the counts first).  mgldg_disk_mesh (no
+ * reference counterpart; the reference reads distmesh output) meshes the
+ * unit disk with concentric rings of spacing 1/ceil(1/h), same calling
+ * pattern. */
+int mgldg_mesh_read(const char* path, int* np, int* nt, double* p, int* t);
+int mgldg_disk_mesh(double h, int* np, int* nt, double* p, int* t);
+/* P_{P-1} LDG on a triangle mesh (Mesh(wireframe), mesh.h:187-300;
+ * LDGPoisson::discretize, ldgpoisson.tpp:27-100), homogeneous Dirichlet on
+ * every boundary edge, P in 1..4 (b = P(P+1)/2 unknowns per element), with
+ * an agglomeration hierarchy of up to agg_levels levels
+ * (InterpolationHierarchy(agglomeration), interpolationhierarchy.h:89-210:
+ * tensor-product Q_{P-1} spaces on the aggregates' bounding boxes, so the
+ * first transfer has b x P^2 blocks).  The aggregates come from a greedy
+ * seeded agglomeration of at most four elements (plus merged singletons)
+ * in place of MGridGen.  mgldg_problem_rhs_gaussian(_dev) on such a problem
+ * draws the Gaussian centres uniformly on the unit disk; seed 0 gives f = 1. */
+int mgldg_simplex_problem_create(mgldg_ctx* ctx, int np, const double* p, int nt, const int* t, int P,
+                                 double tau0, double tauD, int agg_levels, uint64_t agg_seed,
+                                 mgldg_problem** out);
+/* Aggregate of every element of agglomeration level l's finer mesh (agg may
+ * be NULL to get the count). */
+int mgldg_problem_partition(const mgldg_problem* pr, int l, int* n, int* agg);
+/* Master simplex (N = 1 or 2): mass, differentiation matrices (row-major
+ * b x b) and nodes (b x N) in the reference's node order. */
+int mgldg_simplex_master(int N, int P, double* mass, double* diff0, double* diff1, double* nodes);
+
 /* ---------------------------------------------------------- file formats -- */
 /* Matrix Market dump of a BSR matrix, the format of the reference's
  * SparseBlockMatrix::write (sparseblockmatrix.tpp:145-164): coordinate real

@@ -401,6 +401,10 @@ static mgldg_problem* cartesian_create(mgldg_ctx* ctx, int P, int n, double tau0
 }
 
 static void rhs_gaussian_dev(mgldg_ctx* ctx, mgldg_problem* pr, uint64_t seed, double* b) {
+    if (pr->simplex) {
+        simplex_rhs_dev(ctx, pr, seed, b);
+        return;
+    }
     Gauss8 g = gaussian_params(seed);
     GaussDev gd;
     std::memcpy(gd.cx, g.cx, sizeof g.cx);
@@ -442,6 +446,30 @@ void problem_boxes(const mgldg_problem* pr, int* P, int* ne, const double** ex, 
     *ex = pr->ex.data();
     *ey = pr->ey.data();
     *ew = pr->ew.data();
+}
+
+void problem_node_coords(const mgldg_problem* pr, std::vector<double>& xy) {
+    const int b = pr->b, P = pr->P;
+    xy.assign((size_t)pr->ne * b * 2, 0.0);
+    for (int e = 0; e < pr->ne; ++e) {
+        double* o = &xy[(size_t)e * b * 2];
+        if (pr->simplex) {
+            // Master::dgnodes: p0 + J node (master.h:40-45)
+            const double* g = &pr->sgeom[(size_t)e * 11];
+            for (int i = 0; i < b; ++i) {
+                const double n0 = pr->snodes[2 * i], n1 = pr->snodes[2 * i + 1];
+                o[2 * i] = g[0] + (g[2] * n0 + g[3] * n1);
+                o[2 * i + 1] = g[1] + (g[4] * n0 + g[5] * n1);
+            }
+        } else {
+            const double h = pr->ew[e];
+            for (int i0 = 0; i0 < P; ++i0)
+                for (int i1 = 0; i1 < P; ++i1) {
+                    o[2 * (i0 * P + i1)] = pr->ex[e] + h * kNodes[P - 1][i0];
+                    o[2 * (i0 * P + i1) + 1] = pr->ey[e] + h * kNodes[P - 1][i1];
+                }
+        }
+    }
 }
 
 void problem_upload_geometry(mgldg_ctx* ctx, mgldg_problem* pr) {

@@ -16,7 +16,7 @@
 #include <map>
 
 #include "api.cuh"
-#include "master_tables.inc"
+#include "ldg_build.cuh"
 
 using namespace mg;
 
@@ -95,30 +95,20 @@ extern "C" int mgldg_bsr_read_mtx(mgldg_ctx* ctx, const char* path, int br, int 
     MG_API_END
 }
 
-struct mgldg_problem;
-namespace mg {
-// element boxes of a problem (defined in cartesian.cu)
-void problem_boxes(const mgldg_problem* pr, int* P, int* ne, const double** ex, const double** ey,
-                   const double** ew);
-}
-
 extern "C" int mgldg_problem_write_fun(mgldg_ctx* ctx, const mgldg_problem* pr, const double* u, const char* path) {
     MG_API_BEGIN(ctx)
     MG_REQUIRE(pr && u && path, MGLDG_ERR_ARG, "null argument");
-    int P = 0, ne = 0;
-    const double *ex = nullptr, *ey = nullptr, *ew = nullptr;
-    problem_boxes(pr, &P, &ne, &ex, &ey, &ew);
-    const int b = P * P;
+    std::vector<double> xy;
+    problem_node_coords(pr, xy);
+    const int b = pr->b;
     FILE* f = std::fopen(path, "w");
     MG_REQUIRE(f != nullptr, MGLDG_ERR_ARG, std::string("cannot open ") + path);
-    std::fprintf(f, "%d %d %d\n", P, 2, ne);
-    for (int e = 0; e < ne; ++e) {
-        const double lo[2] = {ex[e], ey[e]}, h = ew[e];
-        for (int i0 = 0; i0 < P; ++i0)
-            for (int i1 = 0; i1 < P; ++i1) {
-                const double x = lo[0] + h * kNodes[P - 1][i0], y = lo[1] + h * kNodes[P - 1][i1];
-                std::fprintf(f, "%.17g %.17g %.17g\n", x, y, u[(size_t)e * b + i0 * P + i1]);
-            }
+    std::fprintf(f, "%d %d %d\n", pr->P, 2, pr->ne);
+    for (int e = 0; e < pr->ne; ++e) {
+        for (int i = 0; i < b; ++i) {
+            const size_t k = (size_t)e * b + i;
+            std::fprintf(f, "%.17g %.17g %.17g\n", xy[2 * k], xy[2 * k + 1], u[k]);
+        }
         std::fprintf(f, "\n");
     }
     const bool ok = std::fclose(f) == 0;

@@ -151,6 +151,12 @@ struct mgldg_problem {
     double* d_nodes = nullptr;
     double* d_Mref = nullptr;         // tensor mass of the master element
     int nfaces = 0, nbfaces = 0, nlevels = 0;
+    // triangle meshes: per element p0, J, Jinv, volume (11 doubles), the
+    // master nodes (b x 2), the master volume and the aggregates per level
+    bool simplex = false;
+    std::vector<double> sgeom, snodes;
+    double svref = 0;
+    std::vector<std::vector<int>> partitions;
     ~mgldg_problem() {
         delete ops;
         for (auto* t : T) delete t;
@@ -163,4 +169,9 @@ struct mgldg_problem {
 namespace mg {
 // uploads geometry, nodes and the master mass matrix of a built problem
 void problem_upload_geometry(mgldg_ctx* ctx, mgldg_problem* pr);
+// right-hand side b = M f (disk Gaussian sum of seed; seed 0: f = 1) on a
+// triangle mesh (simplex.cu)
+void simplex_rhs_dev(mgldg_ctx* ctx, const mgldg_problem* pr, uint64_t seed, double* b);
+// coordinates of every DOF's node, (x, y) pairs in DOF order
+void problem_node_coords(const mgldg_problem* pr, std::vector<double>& xy);
 }  // namespace mg

@@ -41,7 +41,8 @@ EXPORTS = [
     "mgldg_bsr_mm_dev", "mgldg_mg_vcycle_batched_dev", "mgldg_pcg_batched_dev", "mgldg_pcg_batched",
     "mgldg_mg_batch_tiles", "mgldg_quadtree_create", "mgldg_quadtree_destroy", "mgldg_quadtree_info",
     "mgldg_quadtree_layer", "mgldg_h_points", "mgldg_seeded_points", "mgldg_quadtree_problem_create",
-    "mgldg_problem_mesh_info",
+    "mgldg_problem_mesh_info", "mgldg_mesh_read", "mgldg_disk_mesh", "mgldg_simplex_problem_create",
+    "mgldg_problem_partition", "mgldg_simplex_master",
 ]
 
 
@@ -157,6 +158,12 @@ def lib():
         L.mgldg_seeded_points.argtypes = [C.c_uint64, C.c_int, _dp]
         L.mgldg_quadtree_problem_create.argtypes = [vp, vp, C.c_int, C.c_double, C.c_double, C.c_int, pvp]
         L.mgldg_problem_mesh_info.argtypes = [vp, ip, ip, ip]
+        L.mgldg_mesh_read.argtypes = [C.c_char_p, ip, ip, vp, vp]
+        L.mgldg_disk_mesh.argtypes = [C.c_double, ip, ip, vp, vp]
+        L.mgldg_simplex_problem_create.argtypes = [vp, C.c_int, _dp, C.c_int, _ip, C.c_int, C.c_double, C.c_double,
+                                                   C.c_int, C.c_uint64, pvp]
+        L.mgldg_problem_partition.argtypes = [vp, C.c_int, ip, vp]
+        L.mgldg_simplex_master.argtypes = [C.c_int, C.c_int, _dp, vp, vp, _dp]
         _lib = L
     return _lib
 
@@ -556,13 +563,53 @@ class Quadtree:
             self.h = None
 
 
+def _two_call(fn, *head):
+    np_, nt = C.c_int(), C.c_int()
+    rc = fn(*head, C.byref(np_), C.byref(nt), None, None)
+    if rc:
+        raise MgldgError(rc, "mesh")
+    p = np.zeros((np_.value, 2))
+    t = np.zeros((nt.value, 3), np.int32)
+    rc = fn(*head, C.byref(np_), C.byref(nt), p.ctypes.data_as(C.c_void_p), t.ctypes.data_as(C.c_void_p))
+    if rc:
+        raise MgldgError(rc, "mesh")
+    return p, t
+
+
+def disk_mesh(h):
+    """Triangles of the unit disk with spacing about h: (points[np,2], triangles[nt,3])."""
+    return _two_call(lib().mgldg_disk_mesh, C.c_double(h))
+
+
+def read_mesh(path):
+    """The reference's .mesh wireframe: (points[np,2], triangles[nt,3], 0-based)."""
+    return _two_call(lib().mgldg_mesh_read, str(path).encode())
+
+
+def simplex_master(N, P):
+    b = P if N == 1 else P * (P + 1) // 2
+    mass, d0, d1, nodes = np.zeros(b * b), np.zeros(b * b), np.zeros(b * b), np.zeros(b * N)
+    rc = lib().mgldg_simplex_master(N, P, mass, d0.ctypes.data_as(C.c_void_p), d1.ctypes.data_as(C.c_void_p), nodes)
+    if rc:
+        raise MgldgError(rc, "simplex_master")
+    return mass.reshape(b, b), [d0.reshape(b, b), d1.reshape(b, b)][:N], nodes.reshape(b, N)
+
+
 class CartesianProblem:
     """Uniform n x n quadtree mesh, Q_{P-1} LDG operators and hierarchy, built on the GPU
     (or, with quadtree=..., the leaves of an adaptive Quadtree)."""
 
-    def __init__(self, ctx, P, n=None, tau0=None, tauD=None, quadtree=None, tau_per_face=False):
+    def __init__(self, ctx, P, n=None, tau0=None, tauD=None, quadtree=None, tau_per_face=False, mesh=None,
+                 agg_levels=8, agg_seed=4000):
         h = C.c_void_p()
-        if quadtree is None:
+        if mesh is not None:
+            pts, tris = mesh
+            pts = np.ascontiguousarray(pts, np.float64).ravel()
+            tris = np.ascontiguousarray(tris, np.int32).ravel()
+            ctx.check(lib().mgldg_simplex_problem_create(ctx.h, len(pts) // 2, pts, len(tris) // 3, tris, P,
+                                                         float(tau0), float(tauD), agg_levels, agg_seed,
+                                                         C.byref(h)), "simplex_problem_create")
+        elif quadtree is None:
             tau0 = float(n) if tau0 is None else tau0
             tauD = float(n) if tauD is None else tauD
             ctx.check(lib().mgldg_cartesian_create(ctx.h, P, n, tau0, tauD, C.byref(h)), "cartesian_create")
@@ -587,6 +634,14 @@ class CartesianProblem:
             t = C.c_void_p()
             ctx.check(lib().mgldg_problem_interp(h, l, C.byref(t)), "problem_interp")
             self.T.append(SparseBlockMatrix(ctx, t, owned=False))
+
+    def partition(self, l):
+        n = C.c_int()
+        self.ctx.check(lib().mgldg_problem_partition(self.h, l, C.byref(n), None), "partition")
+        a = np.zeros(n.value, np.int32)
+        self.ctx.check(lib().mgldg_problem_partition(self.h, l, C.byref(n), a.ctypes.data_as(C.c_void_p)),
+                       "partition")
+        return a
 
     def write_fun(self, u, path):
         """Nodal dump of u (the reference's Function::write format)."""

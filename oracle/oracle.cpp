@@ -21,12 +21,14 @@
 #include "oracle.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <fstream>
 #include <functional>
 #include <limits>
+#include <map>
 #include <memory>
 #include <random>
 #include <stdexcept>
@@ -909,6 +911,11 @@ struct Problem {
     std::vector<double> rhs, utrue;
     std::vector<std::vector<Mat>> Tl;   // unused placeholder
     std::vector<SBM> hier;             // InterpolationHierarchy<2,P>::T
+    // simplex meshes (no quadtree / Cartesian mesh)
+    bool simplex = false;
+    int s_ne = 0, s_nf = 0, s_nb = 0;
+    std::vector<std::vector<int>> agg;   // per agglomeration level: aggregate of each finer element
+    std::vector<double> s_xy;            // node coordinates (x, y) in DOF order
 };
 
 // LDGPoisson<N,P>::discretize (ldgpoisson.tpp:14-24) and its parts
@@ -1486,6 +1493,8 @@ struct orc_sbm { SBM s; };
 
 #define ORC_TRY(...) try { __VA_ARGS__; return 0; } catch (...) { return 1; }
 
+#include "unstructured.inc"
+
 extern "C" {
 
 int orc_master_tables(int P, double* nodes, double* denom, double* mass, double* invmass, double* diff) {
@@ -1568,13 +1577,13 @@ int orc_problem_info(const orc_problem* pr, int* ne, int* npl, int* ndof, int* n
                      int* nbfaces) {
     ORC_TRY({
         const Problem& p = *pr->p;
-        int e = (int)p.mesh->elements.size();
+        int e = p.simplex ? p.s_ne : (int)p.mesh->elements.size();
         if (ne) *ne = e;
         if (npl) *npl = p.npl;
         if (ndof) *ndof = e * p.npl;
-        if (nlevels) *nlevels = p.qt->numLevels;
-        if (nfaces) *nfaces = (int)p.mesh->faces.size();
-        if (nbfaces) *nbfaces = p.mesh->nb;
+        if (nlevels) *nlevels = p.simplex ? (int)p.hier.size() + 1 : p.qt->numLevels;
+        if (nfaces) *nfaces = p.simplex ? p.s_nf : (int)p.mesh->faces.size();
+        if (nbfaces) *nbfaces = p.simplex ? p.s_nb : p.mesh->nb;
     })
 }
 int orc_problem_elements(const orc_problem* pr, double* lower, double* upper) {
@@ -1767,6 +1776,19 @@ int orc_problem_write_fun(const orc_problem* pr, const double* u, const char* pa
         const Tables& T = tables(p.P);
         std::ofstream ofs(path);
         ofs.precision(std::numeric_limits<double>::max_digits10);
+        if (p.simplex) {
+            // unstructured Function::write (src/unstructured/dg/function.h:159-176)
+            ofs << p.P << " " << NDIM << " " << p.s_ne << std::endl;
+            for (int e = 0; e < p.s_ne; ++e) {
+                for (int i = 0; i < p.npl; ++i) {
+                    size_t k = (size_t)e * p.npl + i;
+                    ofs << p.s_xy[2 * k] << " " << p.s_xy[2 * k + 1] << " " << u[k] << std::endl;
+                }
+                ofs << std::endl;
+            }
+            if (!ofs) throw std::runtime_error("write failed");
+            return 0;
+        }
         int ne = (int)p.mesh->elements.size();
         ofs << p.P << " " << NDIM << " " << ne << std::endl;
         for (int e = 0; e < ne; ++e) {

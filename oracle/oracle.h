@@ -68,6 +68,18 @@ int orc_problem_create_points(int P, int base_level, int extra_levels, int npoin
                               double radius, int balance, int tau_per_face, double tau0, double tauD,
                               uint64_t rhs_seed, orc_problem** out);
 int orc_seeded_points(uint64_t seed, int n, double* xy);
+/* Unstructured P_{P-1} LDG on a triangle mesh (points p[2*np], triangles
+ * t[3*nt], 0-based), homogeneous Dirichlet on every boundary face, rhs = M f
+ * with the disk Gaussian-sum forcing of rhs_seed, and an agglomeration
+ * hierarchy of up to agg_levels levels (greedy seeded aggregates of <= 4,
+ * tensor-product coarse spaces on the aggregates' bounding boxes). */
+int orc_simplex_problem_create(int np, const double* p, int nt, const int* t, int P, double tau0, double tauD,
+                               int agg_levels, uint64_t agg_seed, uint64_t rhs_seed, orc_problem** out);
+/* block shape of hierarchy level l; aggregate of every finer element at agglomeration level l */
+int orc_hier_block(const orc_problem* pr, int l, int* br, int* bc);
+int orc_problem_partition(const orc_problem* pr, int l, int* agg);
+/* simplex master element (N = 1 or 2): mass, diff matrices (row-major npl x npl), nodes[npl*N] */
+int orc_simplex_master(int N, int P, double* mass, double* diff0, double* diff1, double* nodes);
 int orc_problem_destroy(orc_problem* pr);
 /* ne, npl (=P^2), number of DOFs, number of quadtree levels, faces, boundary faces */
 int orc_problem_info(const orc_problem* pr, int* ne, int* npl, int* ndof,

@@ -82,6 +82,11 @@ def lib():
         L.orc_problem_create_points.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_double,
                                                 C.c_int, C.c_int, C.c_double, C.c_double, C.c_uint64, pvp]
         L.orc_seeded_points.argtypes = [C.c_uint64, C.c_int, _dp]
+        L.orc_simplex_problem_create.argtypes = [C.c_int, _dp, C.c_int, _ip, C.c_int, C.c_double, C.c_double,
+                                                 C.c_int, C.c_uint64, C.c_uint64, pvp]
+        L.orc_hier_block.argtypes = [vp, C.c_int, ip, ip]
+        L.orc_problem_partition.argtypes = [vp, C.c_int, _ip]
+        L.orc_simplex_master.argtypes = [C.c_int, C.c_int, _dp, vp, vp, _dp]
         _lib = L
     return _lib
 
@@ -103,6 +108,16 @@ def quadrature(Q):
     x, w = np.zeros(Q), np.zeros(Q)
     _ck(lib().orc_quadrature(Q, x, w), "quadrature")
     return x, w
+
+
+def simplex_master(N, P):
+    """(mass, diff[N], nodes) of the master simplex (unstructured master.h)."""
+    npl = {1: P, 2: P * (P + 1) // 2}[N]
+    mass, d0, d1, nodes = np.zeros(npl * npl), np.zeros(npl * npl), np.zeros(npl * npl), np.zeros(npl * N)
+    _ck(lib().orc_simplex_master(N, P, mass, d0.ctypes.data_as(C.c_void_p), d1.ctypes.data_as(C.c_void_p), nodes),
+        "simplex_master")
+    diffs = [d0.reshape(npl, npl), d1.reshape(npl, npl)][:N]
+    return mass.reshape(npl, npl), diffs, nodes.reshape(npl, N)
 
 
 def seeded_points(seed, n):
@@ -200,6 +215,26 @@ class Problem:
         self._attach(h, P)
         return self
 
+    @classmethod
+    def simplex(cls, points, tris, P, tau0, tauD, agg_levels=8, agg_seed=4000, seed=4001):
+        """Unstructured P_{P-1} LDG on a triangle mesh (see oracle.h); seed 0: f = 1."""
+        self = cls.__new__(cls)
+        h = C.c_void_p()
+        p = np.ascontiguousarray(points, np.float64).ravel()
+        t = np.ascontiguousarray(tris, np.int32).ravel()
+        _ck(lib().orc_simplex_problem_create(len(p) // 2, p, len(t) // 3, t, P, tau0, tauD, agg_levels, agg_seed,
+                                             seed, C.byref(h)), "simplex_problem_create")
+        self._attach(h, P)
+        return self
+
+    def partition(self, l):
+        sizes = [self.ne]
+        for k in range(l):
+            sizes.append(int(self.partition(k).max()) + 1)
+        agg = np.zeros(sizes[l], np.int32)
+        _ck(lib().orc_problem_partition(self.h, l, agg), "partition")
+        return agg
+
     def _attach(self, h, P):
         self.h = h
         vals = [C.c_int() for _ in range(6)]
@@ -243,12 +278,14 @@ class Problem:
         for l in range(n.value):
             nbr, nbc, nnzb = C.c_int(), C.c_int(), C.c_int()
             _ck(lib().orc_hier_shape(self.h, l, C.byref(nbr), C.byref(nbc), C.byref(nnzb)), "hshape")
+            br, bc = C.c_int(), C.c_int()
+            _ck(lib().orc_hier_block(self.h, l, C.byref(br), C.byref(bc)), "hblock")
+            br, bc = br.value, bc.value
             rp = np.zeros(nbr.value + 1, np.int32)
             ci = np.zeros(nnzb.value, np.int32)
-            v = np.zeros(nnzb.value * self.npl * self.npl)
+            v = np.zeros(nnzb.value * br * bc)
             _ck(lib().orc_hier_export(self.h, l, rp, ci, v), "hexport")
-            out.append(CSR(nbr.value, nbc.value, self.npl, self.npl, rp, ci,
-                           v.reshape(-1, self.npl, self.npl)))
+            out.append(CSR(nbr.value, nbc.value, br, bc, rp, ci, v.reshape(-1, br, bc)))
         return out
 
     def write_mtx(self, which, path):

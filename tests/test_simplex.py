@@ -1,0 +1,125 @@
+"""CPU checks of the unstructured (triangle) path: the master element, the
+disk mesher and .mesh reader (libmgldg host code, no GPU), and the oracle's
+restatement of the reference's unstructured LDG discretisation
+(src/unstructured/dg/ldgpoisson.tpp:27-100) pinned by the reference test's
+exact solution u = (1 - |x|^2)/4 for f = 1 (tests/unstructured/dg_tests.cpp:
+24-25) and by its second-order convergence on polygonal disks.
+"""
+import numpy as np
+import pytest
+
+import oracle_py as O
+
+mgldg = pytest.importorskip("mgldg")
+spla = pytest.importorskip("scipy.sparse.linalg")
+import adjoint_ref as R  # noqa: E402
+
+
+def _lib_or_skip():
+    try:
+        mgldg.lib()
+    except RuntimeError as e:
+        pytest.skip(str(e))
+
+
+@pytest.mark.parametrize("N,P", [(1, 1), (1, 3), (2, 1), (2, 2), (2, 3), (2, 4)])
+def test_master_matches_oracle(N, P):
+    _lib_or_skip()
+    m, d, nodes = mgldg.simplex_master(N, P)
+    mo, do, no = O.simplex_master(N, P)
+    assert np.array_equal(nodes, no)
+    assert np.abs(m - mo).max() <= 1e-15
+    for a, c in zip(d, do):
+        assert np.abs(a - c).max() <= 1e-14 * max(1, np.abs(c).max())
+    # mass integrates 1 to the master volume; rows of diff kill constants
+    vref = 1.0 if N == 1 else 0.5
+    assert abs(m.sum() - vref) <= 1e-15
+    for a in d:
+        assert np.abs(a.sum(axis=1)).max() <= 1e-13
+    # diff of x_k at the nodes is the unit vector (linear functions need P >= 2)
+    for k, a in enumerate(d if P >= 2 else []):
+        for j in range(N):
+            assert np.allclose(a @ nodes[:, j], 1.0 if j == k else 0.0, atol=1e-13)
+
+
+def test_disk_mesh_is_a_conforming_triangulation():
+    _lib_or_skip()
+    p, t = mgldg.disk_mesh(0.05)
+    assert np.all(t >= 0) and np.all(t < len(p))
+    a = p[t[:, 1]] - p[t[:, 0]]
+    b = p[t[:, 2]] - p[t[:, 0]]
+    area = 0.5 * (a[:, 0] * b[:, 1] - a[:, 1] * b[:, 0])
+    assert np.all(area > 0)
+    assert abs(area.sum() - np.pi) < 0.01
+    edges = {}
+    for tri in t:
+        for j in range(3):
+            e = tuple(sorted((tri[j], tri[(j + 1) % 3])))
+            edges[e] = edges.get(e, 0) + 1
+    assert set(edges.values()) <= {1, 2}
+    bverts = {v for e, c in edges.items() if c == 1 for v in e}
+    r = np.linalg.norm(p[list(bverts)], axis=1)
+    assert np.allclose(r, 1.0, atol=1e-14)
+    assert len(p) - len(edges) + len(t) == 1          # Euler characteristic of a disk
+
+
+def test_mesh_file_round_trip(tmp_path):
+    _lib_or_skip()
+    p, t = mgldg.disk_mesh(0.2)
+    path = tmp_path / "disk.mesh"
+    with open(path, "w") as f:
+        f.write(f"{len(p)} {len(t)}\n")
+        f.write("p\n")
+        for x, y in p:
+            f.write(f"{float(x)!r} {float(y)!r}\n")
+        f.write("\n")
+        for tri in t:
+            f.write(f"{tri[0] + 1} {tri[1] + 1} {tri[2] + 1}\n")
+        f.write("\n")
+    q, s = mgldg.read_mesh(path)
+    assert np.array_equal(q, p) and np.array_equal(s, t)
+    bad = tmp_path / "bad.mesh"
+    bad.write_text("3 1\np\n0 0\n1 0\n0 1\n\n1 2 4\n")
+    with pytest.raises(mgldg.MgldgError):
+        mgldg.read_mesh(bad)
+
+
+def _nodes(p, t, P):
+    _, _, nodes = O.simplex_master(2, P)
+    P0 = p[t[:, 0]]
+    J = np.stack([p[t[:, 1]] - P0, p[t[:, 2]] - P0], axis=2)     # ne x 2 x 2
+    return (P0[:, None, :] + np.einsum("eij,qj->eqi", J, nodes)).reshape(-1, 2)
+
+
+def test_oracle_reproduces_the_reference_disk_solution():
+    _lib_or_skip()
+    errs = []
+    for h in (0.2, 0.1, 0.05):
+        p, t = mgldg.disk_mesh(h)
+        pr = O.Problem.simplex(p, t, 3, 1 / h, 1 / h, agg_levels=2, seed=0)
+        A = R.to_scipy(pr.op(O.OP_A)).tocsc()
+        assert abs(A - A.T).max() <= 1e-13 * abs(A).max()
+        u = spla.spsolve(A, pr.rhs())
+        X = _nodes(p, t, 3)
+        errs.append(np.abs(u - (1 - (X ** 2).sum(1)) / 4).max())
+    rates = np.log2(np.array(errs[:-1]) / np.array(errs[1:]))
+    assert errs[-1] < 2e-4 and np.all(rates > 1.8)
+
+
+def test_agglomeration_covers_and_coarsens():
+    _lib_or_skip()
+    p, t = mgldg.disk_mesh(0.05)
+    pr = O.Problem.simplex(p, t, 3, 20.0, 20.0, agg_levels=6)
+    n = pr.ne
+    for l in range(pr.nlevels - 1):
+        a = pr.partition(l)
+        assert len(a) == n
+        counts = np.bincount(a)
+        assert counts.min() >= 1 and len(counts) < n
+        assert np.median(counts) >= 3
+        n = len(counts)
+    H = pr.hierarchy()
+    assert (H[0].br, H[0].bc) == (6, 9) and all((T.br, T.bc) == (9, 9) for T in H[1:])
+    # interpolation of a constant is the constant
+    for T in H:
+        assert np.allclose(T.matvec(np.ones(T.nbc * T.bc)), 1.0, atol=1e-12)
