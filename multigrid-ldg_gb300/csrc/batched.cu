@@ -308,7 +308,9 @@ static bool dispatch_v(mgldg_ctx* ctx, const SpmmArgs<T>& a, const TileCfg& cfg,
     }
 }
 
-static bool is_tiled_shape(int br, int bc) { return br == bc && (br == 4 || br == 9 || br == 16 || br == 25); }
+static bool is_tiled_shape(int br, int bc) {
+    return br == bc && (br == 4 || br == 6 || br == 9 || br == 10 || br == 16 || br == 25);
+}
 
 static bool aligned(const void* p, size_t a) { return p == nullptr || ((uintptr_t)p % a) == 0; }
 
@@ -328,7 +330,7 @@ static void spmm_launch(mgldg_ctx* ctx, int br, int bc, const SpmmArgs<T>& a, in
         bool ok = false;
 #define MG_B(B)                                                                                        \
     if (br == B) ok = mode == 0 ? dispatch_v<T, B, 0>(ctx, a, cfg, kclass) : dispatch_v<T, B, 1>(ctx, a, cfg, kclass);
-        MG_B(4) MG_B(9) MG_B(16) MG_B(25)
+        MG_B(4) MG_B(6) MG_B(9) MG_B(10) MG_B(16) MG_B(25)
 #undef MG_B
         if (ok) return;
     }

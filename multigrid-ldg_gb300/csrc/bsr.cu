@@ -463,8 +463,11 @@ void spmv(mgldg_ctx* ctx, const mgldg_bsr* A, T alpha, const T* x, T beta, const
         return;                                                                                        \
     }
     MG_SPMV_CASE(1, 1)
+    MG_SPMV_CASE(3, 3)
     MG_SPMV_CASE(4, 4)
+    MG_SPMV_CASE(6, 6)
     MG_SPMV_CASE(9, 9)
+    MG_SPMV_CASE(10, 10)
     MG_SPMV_CASE(16, 16)
     MG_SPMV_CASE(25, 25)
 #undef MG_SPMV_CASE

@@ -363,8 +363,11 @@ void gs_sweep(mgldg_ctx* ctx, const mgldg_bsr* A, const T* vals, const T* Dinv, 
     MG_REQUIRE(A->br == A->bc, MGLDG_ERR_SHAPE, "smoother needs square blocks");
     switch (A->br) {
         case 1: launch_gs<T, 1>(ctx, A, vals, Dinv, b, x, S, omega, reverse); return;
+        case 3: launch_gs<T, 3>(ctx, A, vals, Dinv, b, x, S, omega, reverse); return;
         case 4: launch_gs<T, 4>(ctx, A, vals, Dinv, b, x, S, omega, reverse); return;
+        case 6: launch_gs<T, 6>(ctx, A, vals, Dinv, b, x, S, omega, reverse); return;
         case 9: launch_gs<T, 9>(ctx, A, vals, Dinv, b, x, S, omega, reverse); return;
+        case 10: launch_gs<T, 10>(ctx, A, vals, Dinv, b, x, S, omega, reverse); return;
         case 16: launch_gs<T, 16>(ctx, A, vals, Dinv, b, x, S, omega, reverse); return;
         case 25: launch_gs<T, 25>(ctx, A, vals, Dinv, b, x, S, omega, reverse); return;
     }
@@ -397,8 +400,11 @@ void jacobi_sweep(mgldg_ctx* ctx, const mgldg_bsr* A, const T* vals, const T* Di
     }
     switch (A->br) {
         case 1: launch_jacobi<T, 1>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
+        case 3: launch_jacobi<T, 3>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
         case 4: launch_jacobi<T, 4>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
+        case 6: launch_jacobi<T, 6>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
         case 9: launch_jacobi<T, 9>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
+        case 10: launch_jacobi<T, 10>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
         case 16: launch_jacobi<T, 16>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
         case 25: launch_jacobi<T, 25>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
     }

@@ -5,7 +5,8 @@ the .fun dump.
 
 Tolerances: operators 1e-13 of their largest entry; transfers 1e-14;
 right-hand sides 1e-14; PCG histories with the same iteration count and
-every ||r_k|| within 1e-12 ||b||; solutions 1e-10.
+every ||r_k|| within 1e-12 ||b|| (RAT coarsening; RATRAT 1e-8, see the
+test), solutions 1e-10.
 """
 import numpy as np
 import pytest
@@ -68,8 +69,13 @@ def test_simplex_pcg_history_matches_oracle(ctx, relax, omega, restriction):
                          solver=mgldg.COARSE_DENSE, restriction=restriction, mean_project=0)
     xg, hg = mgldg.pcg(ctx, prob.ops.A, b, precon=mg, tol=1e-10)
     assert len(hg) == len(hr) and 5 < len(hr) < 80
-    assert np.abs(hg - hr).max() <= 1e-12 * np.linalg.norm(b)
-    assert np.abs(xg - xr).max() <= 1e-10 * np.abs(xr).max()
+    # RATRAT inverts the coarse mass blocks M_c = T^T M T; on aggregates that
+    # fill a thin part of their bounding box these reach cond ~ 3e8 (0.05
+    # disk, level 1), so the oracle's LDL^T solves and the GPU's inverses
+    # agree to cond * eps only; RAT inverts nothing and keeps 1e-12
+    tol = 1e-12 if restriction == mgldg.RESTRICT_RAT else 1e-8
+    assert np.abs(hg - hr).max() <= tol * np.linalg.norm(b)
+    assert np.abs(xg - xr).max() <= max(1e-10, tol) * np.abs(xr).max()
 
 
 def test_simplex_mixed_precision_and_batched(ctx):
