@@ -321,6 +321,18 @@ int mgldg_pcg_batched_dev(mgldg_ctx* ctx, mgldg_mg* mg, const mgldg_bsr* A, int 
 int mgldg_pcg_batched(mgldg_ctx* ctx, mgldg_mg* mg, const mgldg_bsr* A, int k,
                       const double* B, double* X, double tol, int maxit, int* iters,
                       double* res_hist);
+/* No counterpart in the reference: many independent systems of uneven
+ * sizes solved together.  A holds them as one block-diagonal operator (for
+ * example the LDG operator of a union of meshes, whose multigrid hierarchy
+ * is then block diagonal as well); segment s is unknowns
+ * [seg_offsets[s], seg_offsets[s+1]) (host array of nseg+1 int64).  Every
+ * SpMV and V-cycle covers all segments at once, every segment keeps its own
+ * CG scalars and stopping test (krylov.h:22-68), so segment s reproduces the
+ * pcg of its own system; iters[nseg] and res_hist[s*maxit + i] as in
+ * mgldg_pcg_batched_dev.  Device vectors b, x. */
+int mgldg_pcg_segmented_dev(mgldg_ctx* ctx, mgldg_mg* mg, const mgldg_bsr* A, int nseg,
+                            const int64_t* seg_offsets, const double* b, double* x, double tol, int maxit,
+                            int* iters, double* res_hist);
 /* Column tile widths (32, 64 or 128) the autotuner chose for level `level`'s
  * SpMM, Jacobi sweep, restriction, prolongation and for the outer FP64 SpMM. */
 int mgldg_mg_batch_tiles(const mgldg_mg* mg, int level, int* spmm, int* jacobi, int* restrict_,

@@ -1034,6 +1034,211 @@ static void require_batch(mgldg_mg* m, int k) {
                "the multi-RHS V-cycle smooths with block Jacobi only");
 }
 
+// --------------------------------------------------------- segmented PCG --
+// Many independent systems stored as one block-diagonal operator (a union of
+// meshes): segment s holds unknowns [off[s], off[s+1]).  The SpMV and the
+// V-cycle run over the whole union; every segment keeps its own CG scalars
+// and stopping test, so segment s follows the single-system pcg
+// (krylov.h:22-68) of its own mesh.
+struct SegWork {
+    int nseg = 0;
+    int64_t n = 0;
+    int gx = 0;
+    int64_t* off = nullptr;
+    double *R = nullptr, *D = nullptr, *Q = nullptr, *S = nullptr, *hist = nullptr, *partials = nullptr;
+    int hist_len = 0;
+    BatchScalars sc{};
+    double* sc_mem = nullptr;
+    int* sc_int = nullptr;
+    int* h_counter = nullptr;
+};
+
+void seg_free(SegWork* w) {
+    if (!w) return;
+    dfree(w->off);
+    dfree(w->R); dfree(w->D); dfree(w->Q); dfree(w->S); dfree(w->hist); dfree(w->partials);
+    dfree(w->sc_mem);
+    dfree(w->sc_int);
+    if (w->h_counter) cudaFreeHost(w->h_counter);
+    delete w;
+}
+
+// partials[blockIdx.x * nseg + s] = this CTA's part of segment s of a.b
+__global__ void __launch_bounds__(256) k_segdot(const int64_t* __restrict__ off, int nseg, const double* __restrict__ a,
+                                               const double* __restrict__ b, double* __restrict__ partials) {
+    __shared__ double red[8];
+    const int s = blockIdx.y;
+    const int64_t lo = off[s], hi = off[s + 1];
+    double acc = 0;
+    for (int64_t i = lo + (int64_t)blockIdx.x * 256 + threadIdx.x; i < hi; i += (int64_t)gridDim.x * 256)
+        acc += a[i] * b[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < 8; ++w) t += red[w];
+        partials[(size_t)blockIdx.x * nseg + s] = t;
+    }
+}
+
+// x += alpha_s d ; (r -= alpha_s q) on active segments
+__global__ void __launch_bounds__(256) k_segupdate(const int64_t* __restrict__ off, BatchScalars sc,
+                                                  const double* __restrict__ d, const double* __restrict__ q,
+                                                  double* __restrict__ x, double* __restrict__ r, int update_r) {
+    const int s = blockIdx.y;
+    if (!sc.active[s]) return;
+    const double al = sc.alpha[s];
+    const int64_t lo = off[s], hi = off[s + 1];
+    for (int64_t i = lo + (int64_t)blockIdx.x * 256 + threadIdx.x; i < hi; i += (int64_t)gridDim.x * 256) {
+        x[i] += al * d[i];
+        if (update_r) r[i] -= al * q[i];
+    }
+}
+
+// d = s + beta_s d on active segments
+__global__ void __launch_bounds__(256) k_segdir(const int64_t* __restrict__ off, BatchScalars sc,
+                                               const double* __restrict__ sv, double* __restrict__ d) {
+    const int s = blockIdx.y;
+    if (!sc.active[s]) return;
+    const double be = sc.beta[s];
+    const int64_t lo = off[s], hi = off[s + 1];
+    for (int64_t i = lo + (int64_t)blockIdx.x * 256 + threadIdx.x; i < hi; i += (int64_t)gridDim.x * 256)
+        d[i] = sv[i] + be * d[i];
+}
+
+static SegWork* ensure_seg(mgldg_mg* m, const std::vector<int64_t>& off, int maxit) {
+    mgldg_ctx* ctx = m->ctx;
+    const int nseg = (int)off.size() - 1;
+    const int64_t n = off.back();
+    SegWork* w = m->seg;
+    if (w && (w->nseg != nseg || w->n != n)) {
+        seg_free(w);
+        w = m->seg = nullptr;
+    }
+    if (!w) {
+        w = new SegWork();
+        m->seg = w;
+        w->nseg = nseg;
+        w->n = n;
+        int64_t maxlen = 1;
+        for (int s = 0; s < nseg; ++s) maxlen = std::max<int64_t>(maxlen, off[s + 1] - off[s]);
+        w->gx = (int)std::max<int64_t>(1, std::min<int64_t>((maxlen + 2047) / 2048, 4 * ctx->sm_count / std::max(1, nseg) + 1));
+        w->off = dalloc<int64_t>(nseg + 1);
+        w->R = dalloc<double>(n); w->D = dalloc<double>(n); w->Q = dalloc<double>(n); w->S = dalloc<double>(n);
+        w->partials = dalloc<double>((size_t)w->gx * nseg);
+        w->sc_mem = dalloc<double>(5 * (size_t)nseg);
+        w->sc_int = dalloc<int>(3 * (size_t)nseg + 2);
+        w->sc.delta_new = w->sc_mem;
+        w->sc.delta_old = w->sc_mem + nseg;
+        w->sc.delta0 = w->sc_mem + 2 * nseg;
+        w->sc.alpha = w->sc_mem + 3 * nseg;
+        w->sc.beta = w->sc_mem + 4 * nseg;
+        w->sc.active = w->sc_int;
+        w->sc.iters = w->sc_int + nseg;
+        w->sc.broken = w->sc_int + 2 * nseg;
+        w->sc.counter = w->sc_int + 3 * nseg;
+        MG_CHECK_CUDA(cudaMallocHost(&w->h_counter, 2 * sizeof(int)));
+    }
+    upload(ctx, w->off, off.data(), off.size());
+    const int len = std::max(1, maxit) * nseg;
+    if (w->hist_len < len) {
+        dfree(w->hist);
+        w->hist = nullptr;
+        w->hist = dalloc<double>(len);
+        w->hist_len = len;
+    }
+    return w;
+}
+
+static void segpcg(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const std::vector<int64_t>& off, const double* b,
+                   double* x, double tol, int maxit, int* iters, double* res_hist) {
+    SegWork* w = ensure_seg(m, off, maxit);
+    const int nseg = w->nseg;
+    BatchScalars sc = w->sc;
+    const dim3 grid(w->gx, nseg);
+    const int gk = (nseg + 127) / 128;
+    const double tol2 = tol * tol;
+    auto segdot = [&](const double* a, const double* c) {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_segdot<<<grid, 256, 0, ctx->stream>>>(w->off, nseg, a, c, w->partials);
+    };
+    // R = b - A x ; D = M(R) ; delta = R.D per segment
+    spmv<double>(ctx, A, -1.0, x, 1.0, b, w->R);
+    mg_precon(m, w->R, w->D);
+    segdot(w->R, w->D);
+    check_launch();
+    {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_bpcg_init<<<gk, 128, 0, ctx->stream>>>(nseg, sc, w->partials, w->gx, tol2, maxit);
+    }
+    {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_bpcg_count<<<1, 256, 0, ctx->stream>>>(nseg, sc);
+    }
+    check_launch();
+    MG_CHECK_CUDA(cudaMemcpyAsync(w->h_counter, sc.counter, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    sync(ctx);
+    mg_take_errors(m);
+    int i = 0;
+    while (w->h_counter[0] > 0) {
+        spmv<double>(ctx, A, 1.0, w->D, 0.0, nullptr, w->Q);
+        segdot(w->D, w->Q);
+        {
+            Launch L(ctx, MGLDG_K_VECTOR);
+            k_bpcg_alpha<<<gk, 128, 0, ctx->stream>>>(nseg, sc, w->partials, w->gx);
+        }
+        const bool replace = i % 50 == 0;
+        {
+            Launch L(ctx, MGLDG_K_VECTOR);
+            k_segupdate<<<grid, 256, 0, ctx->stream>>>(w->off, sc, w->D, w->Q, x, w->R, replace ? 0 : 1);
+        }
+        check_launch();
+        if (replace) spmv<double>(ctx, A, -1.0, x, 1.0, b, w->R);
+        segdot(w->R, w->R);
+        {
+            Launch L(ctx, MGLDG_K_VECTOR);
+            k_bpcg_rr<<<gk, 128, 0, ctx->stream>>>(nseg, sc, w->partials, w->gx, w->hist, maxit, i);
+        }
+        check_launch();
+        mg_precon(m, w->R, w->S);
+        segdot(w->R, w->S);
+        {
+            Launch L(ctx, MGLDG_K_VECTOR);
+            k_bpcg_beta<<<gk, 128, 0, ctx->stream>>>(nseg, sc, w->partials, w->gx);
+        }
+        {
+            Launch L(ctx, MGLDG_K_VECTOR);
+            k_segdir<<<grid, 256, 0, ctx->stream>>>(w->off, sc, w->S, w->D);
+        }
+        {
+            Launch L(ctx, MGLDG_K_VECTOR);
+            k_bpcg_end<<<gk, 128, 0, ctx->stream>>>(nseg, sc, tol2, maxit, i);
+        }
+        {
+            Launch L(ctx, MGLDG_K_VECTOR);
+            k_bpcg_count<<<1, 256, 0, ctx->stream>>>(nseg, sc);
+        }
+        check_launch();
+        MG_CHECK_CUDA(cudaMemcpyAsync(w->h_counter, sc.counter, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        sync(ctx);
+        ++i;
+    }
+    mg_take_errors(m);
+    std::vector<int> it(nseg), broken(nseg);
+    download(ctx, it.data(), sc.iters, nseg);
+    download(ctx, broken.data(), sc.broken, nseg);
+    sync(ctx);
+    if (iters) std::copy(it.begin(), it.end(), iters);
+    if (res_hist && maxit > 0) {
+        download(ctx, res_hist, w->hist, (int64_t)maxit * nseg);
+        sync(ctx);
+    }
+    for (int s = 0; s < nseg; ++s)
+        if (broken[s]) throw Error(MGLDG_ERR_BREAKDOWN, "pcg breakdown in segment " + std::to_string(s));
+}
+
 }  // namespace mg
 
 // ================================================================== C ABI ==
@@ -1110,4 +1315,21 @@ extern "C" int mgldg_mg_batch_tiles(const mgldg_mg* m, int level, int* spmm, int
     if (prolong) *prolong = 32 * B.prolong.V;
     if (outer) *outer = 32 * m->batch->outer.V;
     return MGLDG_OK;
+}
+
+extern "C" int mgldg_pcg_segmented_dev(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, int nseg,
+                                       const int64_t* seg_offsets, const double* b, double* x, double tol, int maxit,
+                                       int* iters, double* res_hist) {
+    MG_API_BEGIN(ctx)
+    MG_REQUIRE(m && !m->L.empty(), MGLDG_ERR_ARG, "segmented pcg needs a multigrid preconditioner");
+    MG_REQUIRE(A && b && x && seg_offsets && nseg >= 1 && nseg <= 65535 && maxit >= 0, MGLDG_ERR_ARG,
+               "bad segmented pcg arguments");
+    MG_REQUIRE(A->br == A->bc && A->nbr == A->nbc, MGLDG_ERR_SHAPE, "pcg needs a square matrix");
+    const int64_t n = (int64_t)A->nbr * A->br;
+    MG_REQUIRE(m->L[0].n == n, MGLDG_ERR_SHAPE, "preconditioner size mismatch");
+    std::vector<int64_t> off(seg_offsets, seg_offsets + nseg + 1);
+    MG_REQUIRE(off[0] == 0 && off[nseg] == n, MGLDG_ERR_SHAPE, "segments must cover the unknowns");
+    for (int s = 0; s < nseg; ++s) MG_REQUIRE(off[s + 1] > off[s], MGLDG_ERR_ARG, "empty or unsorted segment");
+    segpcg(ctx, m, A, off, b, x, tol, maxit, iters, res_hist);
+    MG_API_END
 }

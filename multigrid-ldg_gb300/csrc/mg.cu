@@ -374,6 +374,9 @@ static void precon(mgldg_mg* m, const double* r, double* s) {
     vcycle_dev(m, r, s, true);
 }
 
+void mg_precon(mgldg_mg* m, const double* r, double* s) { precon(m, r, s); }
+void mg_take_errors(mgldg_mg* m) { take_errors(m); }
+
 // pcg on device vectors (krylov.h:22-68)
 static void pcg_dev(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const double* b, double* x, double tol,
                     int maxit, int* iters, double* res_hist) {
@@ -473,6 +476,7 @@ mgldg_mg::~mgldg_mg() {
     dfree(sc);
     if (h_sc) cudaFreeHost(h_sc);
     mg::batch_free(batch);
+    mg::seg_free(seg);
 }
 
 // ================================================================== C ABI ==

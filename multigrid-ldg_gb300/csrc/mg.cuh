@@ -44,6 +44,12 @@ struct LV<float> {
 
 struct Batch;
 void batch_free(Batch* b);
+struct SegWork;
+void seg_free(SegWork* w);
+// one preconditioner application s = V-cycle(r) from x = 0 (graph replay
+// when possible) and the collection of device-side error reports (mg.cu)
+void mg_precon(mgldg_mg* m, const double* r, double* s);
+void mg_take_errors(mgldg_mg* m);
 
 struct PcgScalars {
     double delta_new, delta_old, delta0, alpha, beta, dq, rr, pad;
@@ -75,5 +81,6 @@ struct mgldg_mg {
     int next_graph = 0;
     bool graphs_off = false;
     mg::Batch* batch = nullptr;   // multi-RHS work space (batched.cu)
+    mg::SegWork* seg = nullptr;   // segmented-PCG work space (batched.cu)
     ~mgldg_mg();
 };

@@ -347,9 +347,10 @@ typedef std::vector<std::vector<std::pair<int, double>>> Graph;
 // Greedy seeded agglomeration (no reference counterpart; stands in for
 // MGridGen): nodes in the order of seeded keys (mt19937_64(seed), ties by
 // index); an unassigned node starts an aggregate and takes up to three
-// unassigned neighbours, heaviest shared face first (ties: lower index); a
-// remaining singleton joins the neighbour aggregate it shares the heaviest
-// face with (ties: lower neighbour index).  Aggregates keep their creation
+// unassigned neighbours, heaviest shared face first (ties: lower index); an
+// aggregate of fewer than three elements then joins the neighbouring
+// aggregate it shares the most face weight with (ties: lower aggregate;
+// two triangles' nodes need not determine the nine Q2 modes of their box).  Aggregates keep their creation
 // order.
 static std::vector<int> greedy_agglomerate(int n, const Graph& adj, uint64_t seed, int* ncoarse) {
     std::mt19937_64 g(seed);
@@ -376,26 +377,36 @@ static std::vector<int> greedy_agglomerate(int n, const Graph& adj, uint64_t see
             size[a]++;
         }
     }
-    std::vector<int> member(size.size(), -1);
-    for (int u = 0; u < n; ++u)
-        if (size[agg[u]] == 1) member[agg[u]] = u;
+    // aggregates of fewer than three elements join the neighbouring
+    // aggregate they share the most face weight with (ties: lower aggregate)
+    std::vector<std::vector<int>> members(size.size());
+    for (int u = 0; u < n; ++u) members[agg[u]].push_back(u);
     for (int a = 0; a < (int)size.size(); ++a) {
-        if (size[a] != 1) continue;
-        const int u = member[a];
+        if (size[a] == 0 || size[a] >= 3) continue;
+        std::map<int, double> wt;
+        for (int u : members[a])
+            for (auto& e : adj[u]) {
+                const int c = agg[e.first];
+                if (c == a) continue;
+                auto it = wt.find(c);
+                if (it == wt.end()) wt[c] = e.second;
+                else it->second += e.second;
+            }
         int best = -1;
         double bw = -1;
-        for (auto& e : adj[u]) {
-            if (agg[e.first] == a) continue;
-            if (e.second > bw || (e.second == bw && e.first < best)) {
-                bw = e.second;
-                best = e.first;
+        for (auto& kv : wt)
+            if (kv.second > bw) {
+                bw = kv.second;
+                best = kv.first;
             }
+        if (best < 0) continue;
+        for (int u : members[a]) {
+            agg[u] = best;
+            members[best].push_back(u);
         }
-        if (best >= 0) {
-            size[agg[best]]++;
-            size[a] = 0;
-            agg[u] = agg[best];
-        }
+        members[a].clear();
+        size[best] += size[a];
+        size[a] = 0;
     }
     std::vector<int> renum(size.size(), -1);
     int nc = 0;

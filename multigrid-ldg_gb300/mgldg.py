@@ -42,7 +42,7 @@ EXPORTS = [
     "mgldg_mg_batch_tiles", "mgldg_quadtree_create", "mgldg_quadtree_destroy", "mgldg_quadtree_info",
     "mgldg_quadtree_layer", "mgldg_h_points", "mgldg_seeded_points", "mgldg_quadtree_problem_create",
     "mgldg_problem_mesh_info", "mgldg_mesh_read", "mgldg_disk_mesh", "mgldg_simplex_problem_create",
-    "mgldg_problem_partition", "mgldg_simplex_master",
+    "mgldg_problem_partition", "mgldg_simplex_master", "mgldg_pcg_segmented_dev",
 ]
 
 
@@ -164,6 +164,8 @@ def lib():
                                                    C.c_int, C.c_uint64, pvp]
         L.mgldg_problem_partition.argtypes = [vp, C.c_int, ip, vp]
         L.mgldg_simplex_master.argtypes = [C.c_int, C.c_int, _dp, vp, vp, _dp]
+        L.mgldg_pcg_segmented_dev.argtypes = [vp, vp, vp, C.c_int, C.POINTER(C.c_int64), vp, vp, C.c_double,
+                                              C.c_int, _ip, _dp]
         _lib = L
     return _lib
 
@@ -584,6 +586,38 @@ def disk_mesh(h):
 def read_mesh(path):
     """The reference's .mesh wireframe: (points[np,2], triangles[nt,3], 0-based)."""
     return _two_call(lib().mgldg_mesh_read, str(path).encode())
+
+
+def mesh_union(meshes):
+    """Disjoint union of triangle meshes: (points, triangles, element offsets[len+1])."""
+    ps, ts, off, nv, ne = [], [], [0], 0, 0
+    for p, t in meshes:
+        ps.append(np.asarray(p, np.float64))
+        ts.append(np.asarray(t, np.int32) + nv)
+        nv += len(p)
+        ne += len(t)
+        off.append(ne)
+    return np.concatenate(ps), np.concatenate(ts), np.array(off, np.int64)
+
+
+def pcg_segmented(ctx, A, b, seg_offsets, precon, x=None, tol=1e-8, maxit=200):
+    """pcg on independent segments of a block-diagonal system (host vectors):
+    (x, iterations[nseg], [history of segment s])."""
+    import torch
+    b = np.ascontiguousarray(b, np.float64)
+    off = np.ascontiguousarray(seg_offsets, np.int64)
+    nseg = len(off) - 1
+    db = torch.from_numpy(b).to("cuda")
+    dx = torch.from_numpy(np.zeros_like(b) if x is None else np.array(x, np.float64)).to("cuda")
+    torch.cuda.synchronize()
+    its = np.zeros(nseg, np.int32)
+    hist = np.zeros(max(1, maxit) * nseg)
+    rc = lib().mgldg_pcg_segmented_dev(ctx.h, precon.h, A.h, nseg, off.ctypes.data_as(C.POINTER(C.c_int64)),
+                                       C.c_void_p(db.data_ptr()), C.c_void_p(dx.data_ptr()), tol, maxit, its, hist)
+    ctx.check(rc, "pcg_segmented")
+    ctx.sync()
+    hist = hist.reshape(nseg, max(1, maxit))
+    return dx.cpu().numpy(), its, [hist[s, :its[s]].copy() for s in range(nseg)]
 
 
 def simplex_master(N, P):

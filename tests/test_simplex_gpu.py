@@ -99,3 +99,32 @@ def test_simplex_write_fun_matches_oracle(ctx, tmp_path):
     prob.write_fun(u, tmp_path / "ours.fun")
     pr.write_fun(u, tmp_path / "ref.fun")
     assert open(tmp_path / "ours.fun").read() == open(tmp_path / "ref.fun").read()
+
+
+@pytest.mark.parametrize("restriction", [mgldg.RESTRICT_RAT, mgldg.RESTRICT_RATRAT])
+def test_segmented_pcg_on_a_union_of_meshes(ctx, restriction):
+    # three disks of uneven sizes as one block-diagonal system; segment s must
+    # follow the oracle's pcg of the union with b zero outside segment s
+    # (A and the V-cycle are block diagonal, so that is segment s's own solve)
+    meshes = [mgldg.disk_mesh(h) for h in (0.1, 0.2, 0.13)]
+    p, t, eoff = mgldg.mesh_union(meshes)
+    P, tau = 3, 10.0
+    prob = mgldg.CartesianProblem(ctx, P, mesh=(p, t), tau0=tau, tauD=tau, agg_levels=6, agg_seed=4000)
+    pr = O.Problem.simplex(p, t, P, tau, tau, agg_levels=6, agg_seed=4000, seed=4001)
+    b = pr.rhs()
+    off = eoff * prob.npl
+    kw = dict(relaxation=mgldg.RELAX_JACOBI, omega=0.7, npre=2, npost=2, restriction=restriction, mean_project=0)
+    mg = mgldg.Multigrid(ctx, prob.ops, prob.T, solver=mgldg.COARSE_DENSE, **kw)
+    omg = O.Multigrid(pr, relaxation=O.RELAX_JACOBI, omega=0.7, npre=2, npost=2, solver=O.COARSE_DENSE,
+                      restriction=restriction, mean_project=False)
+    x, its, hist = mgldg.pcg_segmented(ctx, prob.ops.A, b, off, precon=mg, tol=1e-10)
+    tol = 1e-12 if restriction == mgldg.RESTRICT_RAT else 1e-8
+    for s in range(len(meshes)):
+        bs = np.zeros_like(b)
+        bs[off[s]:off[s + 1]] = b[off[s]:off[s + 1]]
+        xr, hr, _ = pr.pcg(bs, mg=omg, tol=1e-10)
+        assert its[s] == len(hr) > 3
+        nb = np.linalg.norm(bs)
+        assert np.abs(hist[s] - hr).max() <= tol * nb
+        seg = slice(off[s], off[s + 1])
+        assert np.abs(x[seg] - xr[seg]).max() <= max(1e-10, tol) * np.abs(xr[seg]).max()
