@@ -325,6 +325,128 @@ def run_batched(args, ctx, ext, torch, local, ws):
     return out
 
 
+def _coarse_levels(prob, max_dense=4096):
+    """Levels to keep so that the coarsest agglomerated level fits the dense solve."""
+    n = prob.ne * prob.npl
+    for l in range(len(prob.T)):
+        if n <= max_dense:
+            return l + 1
+        n = (int(prob.partition(l).max()) + 1) * prob.T[l].info()[3]
+    return len(prob.T) + 1
+
+
+def run_unstructured(args, ctx, ext, torch, local, ws):
+    """Unstructured P2 triangles on the unit disk (ring mesher, spacing h):
+    one mesh at h = 0.004 and an uneven batch of 48 disks with h drawn from
+    U[0.01, 0.04] (seed 4000) solved together by the segmented PCG; each mesh
+    with its own seeded disk Gaussian-sum forcing, tau = 1/h, greedy seeded
+    agglomeration (seed 4000), RATRAT, mixed precision, block Jacobi omega 0.7,
+    V(2,2), dense coarsest solve, tol 1e-10."""
+    import mgldg
+    L = mgldg.lib()
+    P = 3
+    dev = f"cuda:{local}"
+    out = {}
+    steps = max(1, min(args.steps, 3))
+
+    def time_solves(fn):
+        for _ in range(max(1, args.warmup - 1)):
+            fn()
+        ctx.sync()
+        dist_barrier(ws)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        for _ in range(steps):
+            r = fn()
+        e1.record(ext)
+        e1.synchronize()
+        return dist_max(e0.elapsed_time(e1) / steps, ws), r
+
+    # ---- one large mesh ----
+    h = args.disk_h
+    t0 = time.perf_counter()
+    pts, tri = mgldg.disk_mesh(h)
+    prob = mgldg.CartesianProblem(ctx, P, mesh=(pts, tri), tau0=1 / h, tauD=1 / h, agg_levels=12, agg_seed=4000)
+    build_ms = (time.perf_counter() - t0) * 1e3
+    nlev = _coarse_levels(prob)
+    t0 = time.perf_counter()
+    mg = mgldg.Multigrid(ctx, prob.ops, prob.T, npre=2, npost=2, solver=mgldg.COARSE_DENSE, max_levels=nlev,
+                         mean_project=0, relaxation=mgldg.RELAX_JACOBI, omega=0.7, precision=mgldg.PREC_MIXED)
+    setup_ms = (time.perf_counter() - t0) * 1e3
+    b = torch.empty(prob.ndof, dtype=torch.float64, device=dev)
+    x = torch.zeros_like(b)
+    torch.cuda.synchronize()
+    ctx.check(L.mgldg_problem_rhs_gaussian_dev(ctx.h, prob.h, 4001, C.c_void_p(b.data_ptr())), "rhs")
+    ctx.sync()
+    hist = np.zeros(WL["maxit"])
+    A = prob.ops.A
+
+    def solve1():
+        with torch.cuda.stream(ext):
+            x.zero_()
+        it = C.c_int()
+        ctx.check(L.mgldg_pcg_dev(ctx.h, mg.h, A.h, C.c_void_p(b.data_ptr()), C.c_void_p(x.data_ptr()), WL["tol"],
+                                  WL["maxit"], C.byref(it), hist), "pcg")
+        return it.value
+
+    ms, iters = time_solves(solve1)
+    out["single"] = {
+        "workload": (f"unit disk, ring mesh h={h}: {prob.ne:,} triangles, P2 LDG (6 DOF/element, {prob.ndof:,} "
+                     f"DOF), tau=1/h, {nlev} agglomeration levels (dense coarsest), mixed precision, Jacobi "
+                     f"omega=0.7, V(2,2), tol 1e-10"),
+        "ms_per_solve": ms, "iters": iters, "problem_build_ms": build_ms, "mg_setup_ms": setup_ms,
+    }
+    del mg, prob, b, x
+    torch.cuda.empty_cache()
+
+    # ---- uneven batch of meshes ----
+    rng = np.random.default_rng(4000)
+    hs = rng.uniform(0.01, 0.04, args.disk_batch)
+    meshes = [mgldg.disk_mesh(float(v)) for v in hs]
+    pts, tri, eoff = mgldg.mesh_union(meshes)
+    t0 = time.perf_counter()
+    prob = mgldg.CartesianProblem(ctx, P, mesh=(pts, tri), tau0=1 / float(hs.min()), tauD=1 / float(hs.min()),
+                                  agg_levels=12, agg_seed=4000)
+    build_ms = (time.perf_counter() - t0) * 1e3
+    nlev = _coarse_levels(prob)
+    mg = mgldg.Multigrid(ctx, prob.ops, prob.T, npre=2, npost=2, solver=mgldg.COARSE_DENSE, max_levels=nlev,
+                         mean_project=0, relaxation=mgldg.RELAX_JACOBI, omega=0.7, precision=mgldg.PREC_MIXED)
+    off = (eoff * prob.npl).astype(np.int64)
+    nseg = len(meshes)
+    b = torch.empty(prob.ndof, dtype=torch.float64, device=dev)
+    tmp = torch.empty_like(b)
+    x = torch.zeros_like(b)
+    torch.cuda.synchronize()
+    for s in range(nseg):
+        ctx.check(L.mgldg_problem_rhs_gaussian_dev(ctx.h, prob.h, 4001 + s, C.c_void_p(tmp.data_ptr())), "rhs")
+        ctx.sync()
+        b[off[s]:off[s + 1]] = tmp[off[s]:off[s + 1]]
+    torch.cuda.synchronize()
+    its = np.zeros(nseg, np.int32)
+    shist = np.zeros(WL["maxit"] * nseg)
+    offp = off.ctypes.data_as(C.POINTER(C.c_int64))
+
+    def solve_batch():
+        with torch.cuda.stream(ext):
+            x.zero_()
+        ctx.check(L.mgldg_pcg_segmented_dev(ctx.h, mg.h, prob.ops.A.h, nseg, offp, C.c_void_p(b.data_ptr()),
+                                            C.c_void_p(x.data_ptr()), WL["tol"], WL["maxit"], its, shist), "seg")
+        return its.copy()
+
+    ms, it = time_solves(solve_batch)
+    out["uneven_batch"] = {
+        "workload": (f"{nseg} disks, h ~ U[0.01,0.04] (seed 4000), {prob.ne:,} triangles / {prob.ndof:,} DOF in "
+                     f"total ({min(len(t) for _, t in meshes):,}..{max(len(t) for _, t in meshes):,} per mesh), "
+                     f"one block-diagonal union, segmented PCG (per-mesh CG scalars and stopping), {nlev} "
+                     f"agglomeration levels, mixed precision, Jacobi omega=0.7, V(2,2), tol 1e-10 per mesh"),
+        "ms_per_batch": ms, "meshes_per_s": nseg / (ms * 1e-3), "iters_min": int(it.min()), "iters_max": int(it.max()),
+        "problem_build_ms": build_ms,
+    }
+    del mg, prob, b, x, tmp
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_gpu(args, ws, rank, local):
     import torch
     import mgldg
@@ -497,9 +619,10 @@ def run_gpu(args, ws, rank, local):
     e2e_ms = dist_max(float(np.mean(e2e)), ws)
 
     batched = None
+    del mgs
     if args.batched > 0:
-        del mgs
         batched = run_batched(args, ctx, ext, torch, local, ws)
+    unstructured = run_unstructured(args, ctx, ext, torch, local, ws) if args.disk_batch > 0 else None
 
     speedup = {}
     for sm in ("gs", "jacobi"):
@@ -530,6 +653,7 @@ def run_gpu(args, ws, rank, local):
                 "api": "mgldg_pcg (host buffers, pinned)"},
         "roofline": roof,
         "batched": batched,
+        "unstructured": unstructured,
         "gpu_launches": gpu_launches,
         "clocks": clk,
     }
@@ -549,6 +673,8 @@ def main():
     ap.add_argument("--batched", type=int, default=64, help="right-hand sides of the multi-RHS line (0: skip)")
     ap.add_argument("--batched-n", type=int, default=512, help="mesh side of the uniform multi-RHS mesh")
     ap.add_argument("--batched-mesh", default="adaptive", choices=["adaptive", "uniform"])
+    ap.add_argument("--disk-h", type=float, default=0.004, help="mesh size of the single unstructured disk")
+    ap.add_argument("--disk-batch", type=int, default=48, help="meshes in the uneven batch (0: skip the line)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
