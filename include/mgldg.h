@@ -104,7 +104,8 @@ int mgldg_ops_create_A(mgldg_ctx* ctx, mgldg_bsr* A, mgldg_ops** ops);
 /* A = T + sum_d G_d^T M G_d  (construct_laplacian, ldgpoisson.h:34-52),
  * symbolic product on the host, numeric product on the GPU. */
 int mgldg_ops_construct_laplacian(mgldg_ctx* ctx, mgldg_ops* ops);
-/* which: 0=M 1=G0 2=G1 3=T 4=A.  The handle stays owned by ops. */
+/* which: 0=M 1=G0 2=G1 3=T 4=A 5=G2 (three-dimensional meshes).  The handle
+ * stays owned by ops. */
 int mgldg_ops_get(const mgldg_ops* ops, int which, const mgldg_bsr** A);
 int mgldg_ops_destroy(mgldg_ops* ops);
 
@@ -276,12 +277,29 @@ int mgldg_disk_mesh(double h, int* np, int* nt, double* p, int* t);
 int mgldg_simplex_problem_create(mgldg_ctx* ctx, int np, const double* p, int nt, const int* t, int P,
                                  double tau0, double tauD, int agg_levels, uint64_t agg_seed,
                                  mgldg_problem** out);
+/* The same for N = 2 (triangles, p[2*np], t[3*nt]) or N = 3 (tetrahedra,
+ * p[3*np], t[4*nt], P in 1..3, b = P(P+1)(P+2)/6; coarse spaces Q_{P-1}
+ * on aggregate boxes, P^3 per aggregate, aggregates grown breadth-first to
+ * eight tetrahedra, at least six).  The right-hand side's Gaussian centres
+ * are uniform in the unit ball.  Boundary faces use a 10 x 10 collapsed
+ * Gauss rule on the master triangle with weights summing to 1, scaled by the
+ * face area. */
+int mgldg_simplex_problem_create_nd(mgldg_ctx* ctx, int N, int np, const double* p, int nt,
+                                    const int* t, int P, double tau0, double tauD, int agg_levels,
+                                    uint64_t agg_seed, mgldg_problem** out);
+/* Tetrahedra of the unit ball (no reference counterpart): the cube
+ * [-1,1]^3 on an n^3 grid, n = ceil(1.4/h), Kuhn-split into six tetrahedra
+ * per cube, vertices mapped onto the ball by x |x|_inf / |x|_2; p[3*np],
+ * t[4*nt]; NULL arrays return the counts. */
+int mgldg_ball_mesh(double h, int* np, int* nt, double* p, int* t);
 /* Aggregate of every element of agglomeration level l's finer mesh (agg may
  * be NULL to get the count). */
 int mgldg_problem_partition(const mgldg_problem* pr, int l, int* n, int* agg);
 /* Master simplex (N = 1 or 2): mass, differentiation matrices (row-major
  * b x b) and nodes (b x N) in the reference's node order. */
 int mgldg_simplex_master(int N, int P, double* mass, double* diff0, double* diff1, double* nodes);
+/* N = 1..3: diff receives the N differentiation matrices one after the other. */
+int mgldg_simplex_master_nd(int N, int P, double* mass, double* diff, double* nodes);
 
 /* ---------------------------------------------------------- file formats -- */
 /* Matrix Market dump of a BSR matrix, the format of the reference's

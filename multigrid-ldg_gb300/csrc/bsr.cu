@@ -466,10 +466,12 @@ void spmv(mgldg_ctx* ctx, const mgldg_bsr* A, T alpha, const T* x, T beta, const
     MG_SPMV_CASE(3, 3)
     MG_SPMV_CASE(4, 4)
     MG_SPMV_CASE(6, 6)
+    MG_SPMV_CASE(8, 8)
     MG_SPMV_CASE(9, 9)
     MG_SPMV_CASE(10, 10)
     MG_SPMV_CASE(16, 16)
     MG_SPMV_CASE(25, 25)
+    MG_SPMV_CASE(27, 27)
 #undef MG_SPMV_CASE
     int grid = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)A->nbr * br + 255) / 256, ctx->sm_count * 8));
     if (partials) grid = std::min(grid, ctx->n_partials);

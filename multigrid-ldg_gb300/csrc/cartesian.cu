@@ -448,19 +448,21 @@ void problem_boxes(const mgldg_problem* pr, int* P, int* ne, const double** ex, 
     *ew = pr->ew.data();
 }
 
-void problem_node_coords(const mgldg_problem* pr, std::vector<double>& xy) {
+int problem_node_coords(const mgldg_problem* pr, std::vector<double>& xy) {
     const int b = pr->b, P = pr->P;
-    xy.assign((size_t)pr->ne * b * 2, 0.0);
+    const int dim = pr->simplex ? pr->sdim : 2;
+    xy.assign((size_t)pr->ne * b * dim, 0.0);
     for (int e = 0; e < pr->ne; ++e) {
-        double* o = &xy[(size_t)e * b * 2];
+        double* o = &xy[(size_t)e * b * dim];
         if (pr->simplex) {
             // Master::dgnodes: p0 + J node (master.h:40-45)
-            const double* g = &pr->sgeom[(size_t)e * 11];
-            for (int i = 0; i < b; ++i) {
-                const double n0 = pr->snodes[2 * i], n1 = pr->snodes[2 * i + 1];
-                o[2 * i] = g[0] + (g[2] * n0 + g[3] * n1);
-                o[2 * i + 1] = g[1] + (g[4] * n0 + g[5] * n1);
-            }
+            const double* g = &pr->sgeom[(size_t)e * 22];
+            for (int i = 0; i < b; ++i)
+                for (int d = 0; d < dim; ++d) {
+                    double acc = g[3 + d * 3] * pr->snodes[(size_t)dim * i];
+                    for (int j = 1; j < dim; ++j) acc += g[3 + d * 3 + j] * pr->snodes[(size_t)dim * i + j];
+                    o[(size_t)dim * i + d] = g[d] + acc;
+                }
         } else {
             const double h = pr->ew[e];
             for (int i0 = 0; i0 < P; ++i0)
@@ -470,6 +472,7 @@ void problem_node_coords(const mgldg_problem* pr, std::vector<double>& xy) {
                 }
         }
     }
+    return dim;
 }
 
 void problem_upload_geometry(mgldg_ctx* ctx, mgldg_problem* pr) {

@@ -99,15 +99,16 @@ extern "C" int mgldg_problem_write_fun(mgldg_ctx* ctx, const mgldg_problem* pr, 
     MG_API_BEGIN(ctx)
     MG_REQUIRE(pr && u && path, MGLDG_ERR_ARG, "null argument");
     std::vector<double> xy;
-    problem_node_coords(pr, xy);
+    const int dim = problem_node_coords(pr, xy);
     const int b = pr->b;
     FILE* f = std::fopen(path, "w");
     MG_REQUIRE(f != nullptr, MGLDG_ERR_ARG, std::string("cannot open ") + path);
-    std::fprintf(f, "%d %d %d\n", pr->P, 2, pr->ne);
+    std::fprintf(f, "%d %d %d\n", pr->P, dim, pr->ne);
     for (int e = 0; e < pr->ne; ++e) {
         for (int i = 0; i < b; ++i) {
             const size_t k = (size_t)e * b + i;
-            std::fprintf(f, "%.17g %.17g %.17g\n", xy[2 * k], xy[2 * k + 1], u[k]);
+            for (int d = 0; d < dim; ++d) std::fprintf(f, "%.17g ", xy[(size_t)dim * k + d]);
+            std::fprintf(f, "%.17g\n", u[k]);
         }
         std::fprintf(f, "\n");
     }

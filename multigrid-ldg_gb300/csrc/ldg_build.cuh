@@ -151,10 +151,11 @@ struct mgldg_problem {
     double* d_nodes = nullptr;
     double* d_Mref = nullptr;         // tensor mass of the master element
     int nfaces = 0, nbfaces = 0, nlevels = 0;
-    // triangle meshes: per element p0, J, Jinv, volume (11 doubles), the
-    // master nodes (b x 2), the master volume and the aggregates per level
+    // simplex meshes: dimension, per element geometry, the master nodes
+    // (b x N), the master volume and the aggregates per level
     bool simplex = false;
-    std::vector<double> sgeom, snodes;
+    int sdim = 2;
+    std::vector<double> sgeom, snodes;   // 22 doubles per element: p0, J, Jinv, volume
     double svref = 0;
     std::vector<std::vector<int>> partitions;
     ~mgldg_problem() {
@@ -172,6 +173,6 @@ void problem_upload_geometry(mgldg_ctx* ctx, mgldg_problem* pr);
 // right-hand side b = M f (disk Gaussian sum of seed; seed 0: f = 1) on a
 // triangle mesh (simplex.cu)
 void simplex_rhs_dev(mgldg_ctx* ctx, const mgldg_problem* pr, uint64_t seed, double* b);
-// coordinates of every DOF's node, (x, y) pairs in DOF order
-void problem_node_coords(const mgldg_problem* pr, std::vector<double>& xy);
+// coordinates of every DOF's node, dim values per DOF in DOF order
+int problem_node_coords(const mgldg_problem* pr, std::vector<double>& xy);
 }  // namespace mg

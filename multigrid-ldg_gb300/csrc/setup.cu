@@ -706,6 +706,7 @@ extern "C" int mgldg_ops_get(const mgldg_ops* ops, int which, const mgldg_bsr** 
         case 2: *A = ops->G[1]; break;
         case 3: *A = ops->T; break;
         case 4: *A = ops->A; break;
+        case 5: *A = ops->G[2]; break;
         default: return MGLDG_ERR_ARG;
     }
     return *A ? MGLDG_OK : MGLDG_ERR_ARG;

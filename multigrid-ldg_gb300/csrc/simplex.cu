@@ -75,51 +75,59 @@ static LD lfact(int n) {
     return f;
 }
 
-// Master<N,P> for N = 1, 2: equispaced nodes in SimplexRange order (last
-// index fastest, index sum < P), nodal basis phi_i = sum_m C(m,i) x^a y^b
+// Master<N,P> for N = 1, 2, 3: equispaced nodes in SimplexRange order (last
+// index fastest, index sum < P), nodal basis phi_i = sum_m C(m,i) x^a y^b z^c
 struct SMaster {
     int N = 0, P = 0, b = 0;
     double volume = 0;
-    std::vector<std::array<int, 2>> idx;     // node multi-indices
-    std::vector<std::array<int, 2>> mono;    // monomial exponents
+    std::vector<std::array<int, 3>> idx;     // node multi-indices
+    std::vector<std::array<int, 3>> mono;    // monomial exponents
     std::vector<LD> C;                       // b x b, C[m*b + i]
     std::vector<double> nodes;               // b x N
-    std::vector<double> mass, invmass, diff[2];
+    std::vector<double> mass, invmass, diff[3];
     SMaster(int N_, int P_) : N(N_), P(P_) {
         for (int i0 = 0; i0 < P; ++i0)
-            for (int i1 = 0; i1 < (N == 2 ? P - i0 : 1); ++i1) idx.push_back({i0, N == 2 ? i1 : 0});
+            for (int i1 = 0; i1 < (N >= 2 ? P - i0 : 1); ++i1)
+                for (int i2 = 0; i2 < (N >= 3 ? P - i0 - i1 : 1); ++i2)
+                    idx.push_back({i0, N >= 2 ? i1 : 0, N >= 3 ? i2 : 0});
         b = (int)idx.size();
         for (int d = 0; d < P; ++d)
             for (int a = d; a >= 0; --a)
-                if (N == 2) mono.push_back({a, d - a});
-                else if (a == d) mono.push_back({a, 0});
+                for (int c = 0; c <= d - a; ++c) {
+                    const int bb = d - a - c;
+                    if (N == 1 && (bb || c)) continue;
+                    if (N == 2 && c) continue;
+                    mono.push_back({a, bb, c});
+                }
         volume = (double)(1 / lfact(N));
-        std::vector<LD> xn((size_t)b * 2, 0);
+        std::vector<LD> xn((size_t)b * 3, 0);
         for (int q = 0; q < b; ++q)
             for (int d = 0; d < N; ++d)
-                xn[(size_t)q * 2 + d] = (P == 1) ? (LD)1 / 3 : (LD)idx[q][d] / (P - 1);
+                xn[(size_t)q * 3 + d] = (P == 1) ? (LD)1 / 3 : (LD)idx[q][d] / (P - 1);   // simplexNodes<N,1>: 1/3
         for (int q = 0; q < b; ++q)
-            for (int d = 0; d < N; ++d) nodes.push_back((double)xn[(size_t)q * 2 + d]);
+            for (int d = 0; d < N; ++d) nodes.push_back((double)xn[(size_t)q * 3 + d]);
         // V(q, m) = mono_m(x_q); C = V^-1
         C.assign((size_t)b * b, 0);
         for (int q = 0; q < b; ++q)
-            for (int m = 0; m < b; ++m) C[(size_t)q * b + m] = mono_val(m, &xn[(size_t)q * 2]);
+            for (int m = 0; m < b; ++m) C[(size_t)q * b + m] = mono_val(m, &xn[(size_t)q * 3]);
         ld_inverse(C, b);
         // mass: exact monomial integrals over the master simplex
-        auto integral = [&](int a0, int a1) -> LD {
-            if (N == 1) return (LD)1 / (a0 + 1);
-            return lfact(a0) * lfact(a1) / lfact(a0 + a1 + 2);
+        // (a! b! c! / (a + b + c + N)!)
+        auto integral = [&](int a0, int a1, int a2) -> LD {
+            return lfact(a0) * lfact(a1) * lfact(a2) / lfact(a0 + a1 + a2 + N);
         };
         std::vector<LD> Mm((size_t)b * b);
         for (int m = 0; m < b; ++m)
-            for (int n = 0; n < b; ++n) Mm[(size_t)m * b + n] = integral(mono[m][0] + mono[n][0], mono[m][1] + mono[n][1]);
+            for (int n = 0; n < b; ++n)
+                Mm[(size_t)m * b + n] =
+                    integral(mono[m][0] + mono[n][0], mono[m][1] + mono[n][1], mono[m][2] + mono[n][2]);
         std::vector<LD> Ml((size_t)b * b, 0);
         for (int i = 0; i < b; ++i)
             for (int j = 0; j < b; ++j) {
-                LD s = 0;
+                LD sum = 0;
                 for (int m = 0; m < b; ++m)
-                    for (int n = 0; n < b; ++n) s += C[(size_t)m * b + i] * Mm[(size_t)m * b + n] * C[(size_t)n * b + j];
-                Ml[(size_t)i * b + j] = s;
+                    for (int n = 0; n < b; ++n) sum += C[(size_t)m * b + i] * Mm[(size_t)m * b + n] * C[(size_t)n * b + j];
+                Ml[(size_t)i * b + j] = sum;
             }
         mass.resize((size_t)b * b);
         for (size_t k = 0; k < Ml.size(); ++k) mass[k] = (double)Ml[k];
@@ -131,17 +139,16 @@ struct SMaster {
             diff[d].assign((size_t)b * b, 0.0);
             for (int q = 0; q < b; ++q)
                 for (int i = 0; i < b; ++i) {
-                    LD s = 0;
-                    for (int m = 0; m < b; ++m) s += C[(size_t)m * b + i] * dmono_val(m, d, &xn[(size_t)q * 2]);
-                    diff[d][(size_t)q * b + i] = (double)s;
+                    LD sum = 0;
+                    for (int m = 0; m < b; ++m) sum += C[(size_t)m * b + i] * dmono_val(m, d, &xn[(size_t)q * 3]);
+                    diff[d][(size_t)q * b + i] = (double)sum;
                 }
         }
     }
     LD mono_val(int m, const LD* x) const {
         LD v = 1;
-        for (int k = 0; k < mono[m][0]; ++k) v *= x[0];
-        if (N == 2)
-            for (int k = 0; k < mono[m][1]; ++k) v *= x[1];
+        for (int d = 0; d < 3; ++d)
+            for (int k = 0; k < mono[m][d]; ++k) v *= x[d];
         return v;
     }
     LD dmono_val(int m, int d, const LD* x) const {
@@ -149,43 +156,47 @@ struct SMaster {
         if (e == 0) return 0;
         LD v = e;
         for (int k = 0; k < e - 1; ++k) v *= x[d];
-        if (N == 2) {
-            const int o = 1 - d;
-            for (int k = 0; k < mono[m][o]; ++k) v *= x[o];
-        }
+        for (int o = 0; o < 3; ++o)
+            if (o != d)
+                for (int k = 0; k < mono[m][o]; ++k) v *= x[o];
         return v;
     }
-    // nodal basis at x (double in, double out)
+    // nodal basis at x (N doubles in)
     void eval(const double* x, double* out) const {
-        const LD xl[2] = {x[0], N == 2 ? x[1] : 0};
+        LD xl[3] = {0, 0, 0};
+        for (int d = 0; d < N; ++d) xl[d] = x[d];
         for (int i = 0; i < b; ++i) {
-            LD s = 0;
-            for (int m = 0; m < b; ++m) s += C[(size_t)m * b + i] * mono_val(m, xl);
-            out[i] = (double)s;
+            LD sum = 0;
+            for (int m = 0; m < b; ++m) sum += C[(size_t)m * b + i] * mono_val(m, xl);
+            out[i] = (double)sum;
         }
     }
-    int index_of(int i0, int i1) const {
+    int index_of(int i0, int i1, int i2 = 0) const {
         for (int k = 0; k < b; ++k)
-            if (idx[k][0] == i0 && idx[k][1] == i1) return k;
+            if (idx[k][0] == i0 && idx[k][1] == i1 && idx[k][2] == i2) return k;
         return -1;
     }
 };
 
 // ------------------------------------------------------------ GPU kernels
-// per element e (geom: p0 x, p0 y, J00, J01, J10, J11, Jinv00, Jinv01,
-// Jinv10, Jinv11, vol): M_e = Mref vol / vref; G_d(e,e) = sum_j Jinv(j,d) D_j
-__global__ void k_simplex_elem(int ne, int b, const double* __restrict__ geom, const double* __restrict__ Mref,
-                               const double* __restrict__ D0, const double* __restrict__ D1, double vref,
-                               double* __restrict__ out) {
+// Element geometry, 22 doubles per element: p0[3], J[3][3] (J[d][i] =
+// p_{i+1,d} - p_{0,d}), Jinv[3][3], volume.
+constexpr int kGeom = 22;
+
+// per element e: M_e = Mref vol / vref; G_d(e,e) = sum_j Jinv(j,d) D_j
+// (ldgpoisson.tpp:27-60 of the unstructured tree)
+__global__ void k_simplex_elem(int ne, int N, int b, const double* __restrict__ geom, const double* __restrict__ Mref,
+                               const double* __restrict__ D, double vref, double* __restrict__ out) {
     const int bsz = b * b;
     const int64_t total = (int64_t)ne * bsz;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int e = (int)(t / bsz), k = (int)(t - (int64_t)e * bsz);
-        const double* g = geom + (size_t)e * 11;
-        out[(size_t)e * bsz + k] = Mref[k] * (g[10] / vref);
-        for (int d = 0; d < 2; ++d) {
-            double v = g[6 + d] * D0[k];   // Jinv(0, d) D0
-            v += g[8 + d] * D1[k];         // + Jinv(1, d) D1
+        const double* g = geom + (size_t)e * kGeom;
+        const double* Jinv = g + 12;
+        out[(size_t)e * bsz + k] = Mref[k] * (g[21] / vref);
+        for (int d = 0; d < N; ++d) {
+            double v = Jinv[0 * 3 + d] * D[k];
+            for (int j = 1; j < N; ++j) v += Jinv[j * 3 + d] * D[(size_t)j * bsz + k];
             out[((size_t)(1 + d) * ne + e) * bsz + k] = v;
         }
     }
@@ -193,39 +204,40 @@ __global__ void k_simplex_elem(int ne, int b, const double* __restrict__ geom, c
 
 struct FaceDev {
     int left, right;
-    double n0, n1, area, volR;
-    int sl[6], sr[6];   // element node of face node a, left / right
+    double n[3], jac, volR;   // jac = face area / master face volume
+    int sl[10], sr[10];       // element node of face node a, left / right
 };
 
-// per interior face, eight blocks: G_d(R,R) = (n_d MinvR) RR, G_d(R,L) =
-// (-n_d MinvR) RL (d = 0, 1), then T(R,R) = tau RR, T(L,L) = tau LL,
-// T(R,L) = -tau RL, T(L,R) = -tau RL^T, with RR = S_r^T (M1 area) S_r etc.
-__global__ void k_simplex_face(int nf, int b, int P1, const FaceDev* __restrict__ faces,
-                               const double* __restrict__ M1, const double* __restrict__ Minv, double vref,
+// per interior face, 2N + 4 blocks: G_d(R,R) = (n_d MinvR) RR, G_d(R,L) =
+// (-n_d MinvR) RL for d < N, then T(R,R) = tau RR, T(L,L) = tau LL,
+// T(R,L) = -tau RL, T(L,R) = -tau RL^T, with RR = S_r^T (Mf jac) S_r etc.
+// (ldgpoisson.tpp:63-100, mesh.h:270-283)
+__global__ void k_simplex_face(int nf, int N, int b, int P1, const FaceDev* __restrict__ faces,
+                               const double* __restrict__ Mf, const double* __restrict__ Minv, double vref,
                                double tau0, double* __restrict__ out) {
     const int bsz = b * b;
-    const int64_t total = (int64_t)nf * 8 * bsz;
+    const int nk = 2 * N + 4;
+    const int64_t total = (int64_t)nf * nk * bsz;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        const int f = (int)(t / (8 * bsz));
-        const int rem = (int)(t - (int64_t)f * 8 * bsz);
+        const int f = (int)(t / ((int64_t)nk * bsz));
+        const int rem = (int)(t - (int64_t)f * nk * bsz);
         const int kind = rem / bsz, k = rem - kind * bsz;
         const int r = k / b, c = k - r * b;
         const FaceDev& F = faces[f];
         double v = 0;
-        if (kind < 4) {
+        if (kind < 2 * N) {
             // (s n_d MinvR)(S_r^T fm S_x), column c must be a face node of the
             // trial side x (right for RR, left for RL)
             const int d = kind >> 1;
             const bool rl = kind & 1;
-            const double nd = d == 0 ? F.n0 : F.n1;
-            const double s = rl ? -nd : nd;
+            const double s = rl ? -F.n[d] : F.n[d];
             const int* sx = rl ? F.sl : F.sr;
             int cc = -1;
             for (int a = 0; a < P1; ++a)
                 if (sx[a] == c) cc = a;
             if (cc >= 0) {
                 // sum over the element nodes k = sr[a] in ascending order
-                int ord[6];
+                int ord[10];
                 for (int a = 0; a < P1; ++a) ord[a] = a;
                 for (int i = 1; i < P1; ++i)
                     for (int j = i; j > 0 && F.sr[ord[j]] < F.sr[ord[j - 1]]; --j) {
@@ -235,13 +247,13 @@ __global__ void k_simplex_face(int nf, int b, int P1, const FaceDev* __restrict_
                 for (int q = 0; q < P1; ++q) {
                     const int a = ord[q];
                     const double minv = s * (Minv[r * b + F.sr[a]] * jac);
-                    v += minv * (M1[a * P1 + cc] * F.area);
+                    v += minv * (Mf[a * P1 + cc] * F.jac);
                 }
             }
         } else {
-            const int kk = kind - 4;
-            const int* srow = (kk == 1) ? F.sl : (kk == 3 ? F.sl : F.sr);
-            const int* scol = (kk == 0) ? F.sr : (kk == 1 ? F.sl : (kk == 2 ? F.sl : F.sr));
+            const int kk = kind - 2 * N;
+            const int* srow = (kk == 1 || kk == 3) ? F.sl : F.sr;
+            const int* scol = (kk == 0 || kk == 3) ? F.sr : F.sl;
             int ra = -1, cb = -1;
             for (int a = 0; a < P1; ++a) {
                 if (srow[a] == r) ra = a;
@@ -249,75 +261,104 @@ __global__ void k_simplex_face(int nf, int b, int P1, const FaceDev* __restrict_
             }
             if (ra >= 0 && cb >= 0) {
                 // T(L,R) = -tau RL^T: entry (r, c) = -tau fm(c-face-node, r-face-node)
-                const double m = (kk == 3) ? M1[cb * P1 + ra] * F.area : M1[ra * P1 + cb] * F.area;
+                const double m = (kk == 3) ? Mf[cb * P1 + ra] * F.jac : Mf[ra * P1 + cb] * F.jac;
                 const double tau = (kk <= 1) ? tau0 : -tau0;
                 v = tau * m;
             }
         }
-        out[(size_t)f * 8 * bsz + (size_t)kind * bsz + k] = v;
+        out[(size_t)f * nk * bsz + (size_t)kind * bsz + k] = v;
     }
 }
 
-// b_e = M_e f at the element's nodes, f the disk Gaussian sum
+// b_e = M_e f at the element's nodes, f a Gaussian sum centred in the unit
+// ball of dimension N (seed 0: f = 1)
 struct GaussDevS {
-    double cx[8], cy[8], w[8], a[8];
+    double c[3][8], w[8], a[8];
     int constant_one;
 };
-__global__ void k_rhs_simplex(int ne, int b, const double* __restrict__ geom, const double* __restrict__ nodes,
+__global__ void k_rhs_simplex(int ne, int N, int b, const double* __restrict__ geom, const double* __restrict__ nodes,
                               const double* __restrict__ Mref, double vref, GaussDevS g, double* __restrict__ out) {
     extern __shared__ double sf[];
     for (int e = blockIdx.x; e < ne; e += gridDim.x) {
-        const double* gm = geom + (size_t)e * 11;
+        const double* gm = geom + (size_t)e * kGeom;
         for (int q = threadIdx.x; q < b; q += blockDim.x) {
-            const double x = gm[0] + (gm[2] * nodes[2 * q] + gm[3] * nodes[2 * q + 1]);
-            const double y = gm[1] + (gm[4] * nodes[2 * q] + gm[5] * nodes[2 * q + 1]);
-            double s = 0;
+            double x[3] = {0, 0, 0};
+            for (int d = 0; d < N; ++d) {
+                double acc = gm[3 + d * 3 + 0] * nodes[N * q + 0];
+                for (int j = 1; j < N; ++j) acc += gm[3 + d * 3 + j] * nodes[N * q + j];
+                x[d] = gm[d] + acc;
+            }
+            double sum = 0;
             if (g.constant_one) {
-                s = 1.0;
+                sum = 1.0;
             } else {
                 for (int k = 0; k < 8; ++k) {
-                    const double dx = x - g.cx[k], dy = y - g.cy[k];
-                    s += g.a[k] * exp(-(dx * dx + dy * dy) / (2.0 * g.w[k] * g.w[k]));
+                    double r2 = 0;
+                    for (int d = 0; d < N; ++d) {
+                        const double dd = x[d] - g.c[d][k];
+                        r2 += dd * dd;
+                    }
+                    sum += g.a[k] * exp(-r2 / (2.0 * g.w[k] * g.w[k]));
                 }
             }
-            sf[q] = s;
+            sf[q] = sum;
         }
         __syncthreads();
-        const double jac = gm[10] / vref;
+        const double jac = gm[21] / vref;
         for (int r = threadIdx.x; r < b; r += blockDim.x) {
-            double s = 0;
-            for (int c = 0; c < b; ++c) s += (Mref[r * b + c] * jac) * sf[c];
-            out[(size_t)e * b + r] = s;
+            double sum = 0;
+            for (int c = 0; c < b; ++c) sum += (Mref[r * b + c] * jac) * sf[c];
+            out[(size_t)e * b + r] = sum;
         }
         __syncthreads();
     }
 }
 
 // ------------------------------------------------------------ host parts
-struct STri {
-    double p[3][2];
-    double J[2][2], Jinv[2][2], vol;
+struct SEl {
+    double p[4][3];
+    double J[3][3], Jinv[3][3], vol;
 };
 
-static STri make_stri(const double* pts, const int* t) {
-    STri s;
-    for (int j = 0; j < 3; ++j)
-        for (int d = 0; d < 2; ++d) s.p[j][d] = pts[2 * t[j] + d];
-    for (int d = 0; d < 2; ++d)
-        for (int i = 0; i < 2; ++i) s.J[d][i] = s.p[i + 1][d] - s.p[0][d];
-    const double det = s.J[0][0] * s.J[1][1] - s.J[0][1] * s.J[1][0];
-    MG_REQUIRE(det != 0 && std::isfinite(det), MGLDG_ERR_ARG, "degenerate triangle");
-    s.Jinv[0][0] = s.J[1][1] / det;
-    s.Jinv[0][1] = -s.J[0][1] / det;
-    s.Jinv[1][0] = -s.J[1][0] / det;
-    s.Jinv[1][1] = s.J[0][0] / det;
-    s.vol = std::fabs(det) / 2;
+static SEl make_sel(int N, const double* pts, const int* t) {
+    SEl s{};
+    for (int j = 0; j <= N; ++j)
+        for (int d = 0; d < N; ++d) s.p[j][d] = pts[(size_t)N * t[j] + d];
+    for (int d = 0; d < N; ++d)
+        for (int i = 0; i < N; ++i) s.J[d][i] = s.p[i + 1][d] - s.p[0][d];
+    double det;
+    if (N == 2) {
+        det = s.J[0][0] * s.J[1][1] - s.J[0][1] * s.J[1][0];
+        MG_REQUIRE(det != 0 && std::isfinite(det), MGLDG_ERR_ARG, "degenerate triangle");
+        s.Jinv[0][0] = s.J[1][1] / det;
+        s.Jinv[0][1] = -s.J[0][1] / det;
+        s.Jinv[1][0] = -s.J[1][0] / det;
+        s.Jinv[1][1] = s.J[0][0] / det;
+        s.vol = std::fabs(det) / 2;
+    } else {
+        const double(&a)[3][3] = s.J;
+        const double c00 = a[1][1] * a[2][2] - a[1][2] * a[2][1];
+        const double c01 = a[1][2] * a[2][0] - a[1][0] * a[2][2];
+        const double c02 = a[1][0] * a[2][1] - a[1][1] * a[2][0];
+        det = a[0][0] * c00 + a[0][1] * c01 + a[0][2] * c02;
+        MG_REQUIRE(det != 0 && std::isfinite(det), MGLDG_ERR_ARG, "degenerate tetrahedron");
+        s.Jinv[0][0] = c00 / det;
+        s.Jinv[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) / det;
+        s.Jinv[0][2] = (a[0][1] * a[1][2] - a[0][2] * a[1][1]) / det;
+        s.Jinv[1][0] = c01 / det;
+        s.Jinv[1][1] = (a[0][0] * a[2][2] - a[0][2] * a[2][0]) / det;
+        s.Jinv[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) / det;
+        s.Jinv[2][0] = c02 / det;
+        s.Jinv[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) / det;
+        s.Jinv[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) / det;
+        s.vol = std::fabs(det) / 6;
+    }
     return s;
 }
 
-// disk Gaussian sum: centres uniform on the unit disk (rejection from
-// [-1,1]^2), widths U[0.05,0.2], amplitudes N(0,1) (Box-Muller, cosine)
-static GaussDevS gaussian_disk(uint64_t seed) {
+// Gaussian sum in the unit ball: centres by rejection from [-1,1]^N,
+// widths U[0.05,0.2], amplitudes N(0,1) (Box-Muller, cosine branch)
+static GaussDevS gaussian_ball(uint64_t seed, int N) {
     GaussDevS p{};
     if (seed == 0) {
         p.constant_one = 1;
@@ -326,13 +367,15 @@ static GaussDevS gaussian_disk(uint64_t seed) {
     std::mt19937_64 g(seed);
     auto uni = [&]() { return (double)(g() >> 11) * 0x1.0p-53; };
     for (int k = 0; k < 8; ++k) {
-        double x, y;
+        double x[3], r2;
         do {
-            x = 2 * uni() - 1;
-            y = 2 * uni() - 1;
-        } while (x * x + y * y >= 1);
-        p.cx[k] = x;
-        p.cy[k] = y;
+            r2 = 0;
+            for (int d = 0; d < N; ++d) {
+                x[d] = 2 * uni() - 1;
+                r2 += x[d] * x[d];
+            }
+        } while (r2 >= 1);
+        for (int d = 0; d < N; ++d) p.c[d][k] = x[d];
         p.w[k] = 0.05 + 0.15 * uni();
         double u1;
         do { u1 = uni(); } while (u1 <= 0.0);
@@ -346,13 +389,17 @@ typedef std::vector<std::vector<std::pair<int, double>>> Graph;
 
 // Greedy seeded agglomeration (no reference counterpart; stands in for
 // MGridGen): nodes in the order of seeded keys (mt19937_64(seed), ties by
-// index); an unassigned node starts an aggregate and takes up to three
-// unassigned neighbours, heaviest shared face first (ties: lower index); an
-// aggregate of fewer than three elements then joins the neighbouring
-// aggregate it shares the most face weight with (ties: lower aggregate;
-// two triangles' nodes need not determine the nine Q2 modes of their box).  Aggregates keep their creation
-// order.
-static std::vector<int> greedy_agglomerate(int n, const Graph& adj, uint64_t seed, int* ncoarse) {
+// index); an unassigned node starts an aggregate and grows it up to maxsize
+// -- in two dimensions with its own unassigned neighbours, heaviest shared
+// face first (ties: lower index); in three dimensions breadth-first, each
+// time taking the unassigned node with the largest total face weight to the
+// aggregate (ties: lower index).  An aggregate of fewer than minsize
+// elements then joins the neighbouring aggregate it shares the most face
+// weight with (ties: lower aggregate): a few elements' nodes need not
+// determine the P^N tensor modes of their bounding box.  Aggregates keep
+// their creation order.
+static std::vector<int> greedy_agglomerate(int n, const Graph& adj, uint64_t seed, int N, int* ncoarse) {
+    const int maxsize = N == 3 ? 8 : 4, minsize = N == 3 ? 6 : 3;
     std::mt19937_64 g(seed);
     std::vector<std::pair<uint64_t, int>> key(n);
     for (int u = 0; u < n; ++u) key[u] = {g(), u};
@@ -365,24 +412,48 @@ static std::vector<int> greedy_agglomerate(int n, const Graph& adj, uint64_t see
         const int a = (int)size.size();
         size.push_back(1);
         agg[u] = a;
-        cand.clear();
-        for (auto& e : adj[u])
-            if (agg[e.first] < 0) cand.push_back(e);
-        std::sort(cand.begin(), cand.end(), [](const std::pair<int, double>& x, const std::pair<int, double>& y) {
-            if (x.second != y.second) return x.second > y.second;
-            return x.first < y.first;
-        });
-        for (size_t k = 0; k < cand.size() && k < 3; ++k) {
-            agg[cand[k].first] = a;
-            size[a]++;
+        if (N != 3) {
+            cand.clear();
+            for (auto& e : adj[u])
+                if (agg[e.first] < 0) cand.push_back(e);
+            std::sort(cand.begin(), cand.end(), [](const std::pair<int, double>& x, const std::pair<int, double>& y) {
+                if (x.second != y.second) return x.second > y.second;
+                return x.first < y.first;
+            });
+            for (size_t k = 0; k < cand.size() && (int)k < maxsize - 1; ++k) {
+                agg[cand[k].first] = a;
+                size[a]++;
+            }
+        } else {
+            std::map<int, double> front;
+            auto grow = [&](int m) {
+                for (auto& e : adj[m])
+                    if (agg[e.first] < 0) {
+                        auto it = front.find(e.first);
+                        if (it == front.end()) front[e.first] = e.second;
+                        else it->second += e.second;
+                    }
+            };
+            grow(u);
+            while (size[a] < maxsize && !front.empty()) {
+                int best = -1;
+                double bw = -1;
+                for (auto& kv2 : front)
+                    if (kv2.second > bw) {
+                        bw = kv2.second;
+                        best = kv2.first;
+                    }
+                front.erase(best);
+                agg[best] = a;
+                size[a]++;
+                grow(best);
+            }
         }
     }
-    // aggregates of fewer than three elements join the neighbouring
-    // aggregate they share the most face weight with (ties: lower aggregate)
     std::vector<std::vector<int>> members(size.size());
     for (int u = 0; u < n; ++u) members[agg[u]].push_back(u);
     for (int a = 0; a < (int)size.size(); ++a) {
-        if (size[a] == 0 || size[a] >= 3) continue;
+        if (size[a] == 0 || size[a] >= minsize) continue;
         std::map<int, double> wt;
         for (int u : members[a])
             for (auto& e : adj[u]) {
@@ -433,12 +504,8 @@ static Graph coarse_graph(const Graph& adj, const std::vector<int>& agg, int nc)
     return out;
 }
 
-}  // namespace mg
-
-namespace mg {
-
 struct SBox {
-    double lo[2], hi[2];
+    double lo[3], hi[3];
 };
 
 static mgldg_bsr* host_bsr(mgldg_ctx* ctx, int nbr, int nbc, int br, int bc, const std::vector<int>& col,
@@ -455,92 +522,141 @@ static mgldg_bsr* host_bsr(mgldg_ctx* ctx, int nbr, int nbc, int br, int bc, con
     return T;
 }
 
-mgldg_problem* simplex_problem(mgldg_ctx* ctx, int np, const double* pts, int nt, const int* tris, int P, double tau0,
-                               double tauD, int agg_levels, uint64_t agg_seed, std::vector<std::vector<int>>* parts) {
-    MG_REQUIRE(P >= 1 && P <= 4, MGLDG_ERR_UNSUPPORTED, "P must be 1..4 on triangles");
-    MG_REQUIRE(np >= 3 && nt >= 1 && pts && tris, MGLDG_ERR_ARG, "empty mesh");
-    for (int k = 0; k < 3 * nt; ++k)
-        MG_REQUIRE(tris[k] >= 0 && tris[k] < np, MGLDG_ERR_ARG, "vertex index out of range");
-    const SMaster M2(2, P), M1(1, P);
-    const int b = M2.b, P1 = M1.b;
-    std::vector<STri> el(nt);
-    for (int e = 0; e < nt; ++e) el[e] = make_stri(pts, tris + 3 * e);
+// quadrature on the master face (an (N-1)-simplex), weights summing to 1:
+// the 10-point Gauss-Legendre rule on an edge; on a triangle the collapsed
+// 10 x 10 Gauss-Legendre product (Duffy), exact for degree 19
+static void face_rule(int N, std::vector<double>& x, std::vector<double>& w) {
+    x.clear();
+    w.clear();
+    if (N == 2) {
+        for (int q = 0; q < MGLDG_QF; ++q) {
+            x.push_back(kQuadNodes[q]);
+            w.push_back(kQuadWeights[q]);
+        }
+        return;
+    }
+    for (int a = 0; a < MGLDG_QF; ++a)
+        for (int c = 0; c < MGLDG_QF; ++c) {
+            const double u = kQuadNodes[a], v = kQuadNodes[c];
+            x.push_back(u);
+            x.push_back(v * (1 - u));
+            w.push_back(2 * kQuadWeights[a] * kQuadWeights[c] * (1 - u));
+        }
+}
 
-    // ---- faces in first-encounter order (mesh.h:209-300) ----
+mgldg_problem* simplex_problem(mgldg_ctx* ctx, int N, int np, const double* pts, int nt, const int* tris, int P,
+                               double tau0, double tauD, int agg_levels, uint64_t agg_seed,
+                               std::vector<std::vector<int>>* parts) {
+    MG_REQUIRE(N == 2 || N == 3, MGLDG_ERR_ARG, "dimension must be 2 or 3");
+    MG_REQUIRE(P >= 1 && P <= (N == 2 ? 4 : 3), MGLDG_ERR_UNSUPPORTED, "P must be 1..4 on triangles, 1..3 on tetrahedra");
+    MG_REQUIRE(np >= N + 1 && nt >= 1 && pts && tris, MGLDG_ERR_ARG, "empty mesh");
+    MG_REQUIRE(N == 2 || np < (1 << 21), MGLDG_ERR_UNSUPPORTED, "more than 2^21 vertices");
+    const int nv = N + 1;
+    for (int64_t k = 0; k < (int64_t)nv * nt; ++k)
+        MG_REQUIRE(tris[k] >= 0 && tris[k] < np, MGLDG_ERR_ARG, "vertex index out of range");
+    const SMaster MS(N, P), MF(N - 1, P);
+    const int b = MS.b, P1 = MF.b;
+    std::vector<SEl> el(nt);
+    for (int e = 0; e < nt; ++e) el[e] = make_sel(N, pts, tris + (size_t)nv * e);
+
+    // ---- faces in first-encounter order (mesh.h:209-300): face j of an
+    // element has the vertices t[(k+j) % (N+1)], k < N
     struct HF {
-        int left, right, v0, v1;
-        double n[2], area;
-        int sl[6], sr[6];
+        int left, right, v[3];
+        double n[3], area;
+        int sl[10], sr[10];
     };
     std::vector<HF> faces;
-    faces.reserve((size_t)nt * 2);
+    faces.reserve((size_t)nt * (N == 2 ? 2 : 3));
     std::unordered_map<uint64_t, int> f2f;
     f2f.reserve((size_t)nt * 4);
     for (int e = 0; e < nt; ++e)
-        for (int j = 0; j < 3; ++j) {
-            const int a = tris[3 * e + j], c = tris[3 * e + (j + 1) % 3];
-            const uint64_t key = ((uint64_t)std::min(a, c) << 32) | (uint32_t)std::max(a, c);
+        for (int j = 0; j < nv; ++j) {
+            int f[3];
+            for (int k = 0; k < N; ++k) f[k] = tris[(size_t)nv * e + (k + j) % nv];
+            std::sort(f, f + N);
+            const uint64_t key = N == 2 ? (((uint64_t)f[0] << 32) | (uint32_t)f[1])
+                                        : (((uint64_t)f[0] << 42) | ((uint64_t)f[1] << 21) | (uint64_t)f[2]);
             auto it = f2f.find(key);
             if (it == f2f.end()) {
-                HF f{};
-                f.left = e;
-                f.right = -1;
-                f.v0 = std::min(a, c);
-                f.v1 = std::max(a, c);
+                HF h{};
+                h.left = e;
+                h.right = -1;
+                for (int k = 0; k < N; ++k) h.v[k] = f[k];
                 f2f.emplace(key, (int)faces.size());
-                faces.push_back(f);
+                faces.push_back(h);
             } else {
-                MG_REQUIRE(faces[it->second].right < 0, MGLDG_ERR_ARG, "an edge is shared by more than two triangles");
+                MG_REQUIRE(faces[it->second].right < 0, MGLDG_ERR_ARG, "a face is shared by more than two elements");
                 faces[it->second].right = e;
             }
         }
-    // local corner of a vertex in an element: reference coordinates
-    // t0 -> (0,0), t1 -> (1,0), t2 -> (0,1)
     auto local = [&](int e, int v) {
-        for (int i = 0; i < 3; ++i)
-            if (tris[3 * e + i] == v) return i;
+        for (int i = 0; i < nv; ++i)
+            if (tris[(size_t)nv * e + i] == v) return i;
         return -1;
     };
-    const int corner[3][2] = {{0, 0}, {1, 0}, {0, 1}};
+    auto P_ = [&](int v, int d) { return pts[(size_t)N * v + d]; };
     int nb = 0;
     for (HF& f : faces) {
-        const double* p0 = pts + 2 * f.v0;
-        const double* p1 = pts + 2 * f.v1;
-        const double dx = p1[0] - p0[0], dy = p1[1] - p0[1];
-        f.area = std::sqrt(dx * dx + dy * dy);
-        double nrm[2] = {dy, -dx};
-        const double len = std::sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1]);
-        nrm[0] /= len;
-        nrm[1] /= len;
+        double e1[3] = {0, 0, 0}, e2[3] = {0, 0, 0}, nrm[3] = {0, 0, 0};
+        for (int d = 0; d < N; ++d) e1[d] = P_(f.v[1], d) - P_(f.v[0], d);
+        if (N == 2) {
+            nrm[0] = e1[1];
+            nrm[1] = -e1[0];
+            f.area = std::sqrt(e1[0] * e1[0] + e1[1] * e1[1]);
+        } else {
+            for (int d = 0; d < 3; ++d) e2[d] = P_(f.v[2], d) - P_(f.v[0], d);
+            nrm[0] = e1[1] * e2[2] - e1[2] * e2[1];
+            nrm[1] = -(e1[0] * e2[2] - e1[2] * e2[0]);
+            nrm[2] = e1[0] * e2[1] - e1[1] * e2[0];
+            // Simplex<2,3>::volume = sqrt(det(J^T J)) / 2 (geometry.h:66-79)
+            double g00 = 0, g01 = 0, g11 = 0;
+            for (int d = 0; d < 3; ++d) {
+                g00 += e1[d] * e1[d];
+                g01 += e1[d] * e2[d];
+                g11 += e2[d] * e2[d];
+            }
+            f.area = std::sqrt(g00 * g11 - g01 * g01) / 2;
+        }
+        double len = 0;
+        for (int d = 0; d < N; ++d) len += nrm[d] * nrm[d];
+        len = std::sqrt(len);
+        for (int d = 0; d < N; ++d) nrm[d] /= len;
         int a = -1;
-        for (int i = 0; i < 3; ++i) {
-            const int v = tris[3 * f.left + i];
-            if (v != f.v0 && v != f.v1) a = v;
+        for (int i = 0; i < nv; ++i) {
+            const int v = tris[(size_t)nv * f.left + i];
+            bool on = false;
+            for (int k = 0; k < N; ++k) on = on || (v == f.v[k]);
+            if (!on) a = v;
         }
-        const double in[2] = {pts[2 * a] - p0[0], pts[2 * a + 1] - p0[1]};
-        if (nrm[0] * in[0] + nrm[1] * in[1] > 0) {
-            nrm[0] = -nrm[0];
-            nrm[1] = -nrm[1];
-        }
-        f.n[0] = nrm[0];
-        f.n[1] = nrm[1];
+        double dot = 0;
+        for (int d = 0; d < N; ++d) dot += nrm[d] * (P_(a, d) - P_(f.v[0], d));
+        if (dot > 0)
+            for (int d = 0; d < N; ++d) nrm[d] = -nrm[d];
+        for (int d = 0; d < N; ++d) f.n[d] = nrm[d];
         if (f.right < 0) {
             ++nb;
             continue;
         }
-        // slicing: face node a at t = a/(P-1) from v0 to v1 is the element
-        // node (1-t) corner(v0) + t corner(v1)
+        // slicing: face node with multi-index j (barycentrics (P-1-|j|, j) on
+        // the sorted face vertices) is the element node sum_k lambda_k corner_k
         for (int side = 0; side < 2; ++side) {
             const int e = side ? f.right : f.left;
-            const int la = local(e, f.v0), lb = local(e, f.v1);
+            int loc[3];
+            for (int k = 0; k < N; ++k) loc[k] = local(e, f.v[k]);
             for (int q = 0; q < P1; ++q) {
-                int node;
-                if (P == 1) {
-                    node = 0;
-                } else {
-                    const int i0 = corner[la][0] * (P - 1 - q) + corner[lb][0] * q;
-                    const int i1 = corner[la][1] * (P - 1 - q) + corner[lb][1] * q;
-                    node = M2.index_of(i0, i1);
+                int node = 0;
+                if (P > 1) {
+                    int lam[3];
+                    lam[0] = P - 1;
+                    for (int k = 1; k < N; ++k) {
+                        lam[k] = MF.idx[q][k - 1];
+                        lam[0] -= lam[k];
+                    }
+                    int m[3] = {0, 0, 0};
+                    for (int k = 0; k < N; ++k)
+                        if (loc[k] > 0) m[loc[k] - 1] += lam[k];   // corner i is the unit vector e_{i-1}
+                    node = MS.index_of(m[0], m[1], m[2]);
                 }
                 (side ? f.sr : f.sl)[q] = node;
             }
@@ -549,45 +665,57 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int np, const double* pts, int nt
     const int nf = (int)faces.size();
     const int nfi = nf - nb;
 
-    // ---- contributions: elements (M, G0, G1), interior faces (8), boundary (3)
+    // ---- contributions: elements (M, G_d), interior faces (2N + 4),
+    // boundary faces (N + 1)
     std::vector<int> interior, boundary;
     for (int k = 0; k < nf; ++k) (faces[k].right >= 0 ? interior : boundary).push_back(k);
     std::vector<int> slot(nf);
     for (int q = 0; q < nfi; ++q) slot[interior[q]] = q;
     for (int q = 0; q < nb; ++q) slot[boundary[q]] = q;
     const size_t bsz = (size_t)b * b;
-    const int64_t c_elem = 0, c_face = (int64_t)3 * nt, c_bnd = c_face + (int64_t)8 * nfi;
-    const int64_t ncontrib = c_bnd + (int64_t)3 * nb;
+    const int nkf = 2 * N + 4, nkb = N + 1;
+    const int64_t c_elem = 0, c_face = (int64_t)(1 + N) * nt, c_bnd = c_face + (int64_t)nkf * nfi;
+    const int64_t ncontrib = c_bnd + (int64_t)nkb * nb;
+    MG_REQUIRE(ncontrib < (int64_t)1 << 31, MGLDG_ERR_UNSUPPORTED, "mesh too large for the contribution index");
 
-    // boundary blocks on the host (quadrature, mesh.h:312-351)
-    std::vector<double> bvals((size_t)3 * nb * bsz);
+    // boundary blocks on the host (quadrature, mesh.h:284-300)
+    std::vector<double> qx, qw;
+    face_rule(N, qx, qw);
+    const int nq = (int)qw.size();
+    std::vector<double> bvals((size_t)nkb * nb * bsz);
     {
-        std::vector<double> phl((size_t)MGLDG_QF * b), Lm((size_t)b * MGLDG_QF), LL(bsz), Minv(bsz);
+        std::vector<double> phl((size_t)nq * b), Lm((size_t)b * nq), LL(bsz), Minv(bsz);
         for (int q = 0; q < nb; ++q) {
             const HF& f = faces[boundary[q]];
-            const STri& s = el[f.left];
-            const double* p0 = pts + 2 * f.v0;
-            const double* p1 = pts + 2 * f.v1;
-            for (int k = 0; k < MGLDG_QF; ++k) {
-                const double phys[2] = {p0[0] + (p1[0] - p0[0]) * kQuadNodes[k], p0[1] + (p1[1] - p0[1]) * kQuadNodes[k]};
-                const double rel[2] = {phys[0] - s.p[0][0], phys[1] - s.p[0][1]};
-                const double xl[2] = {s.Jinv[0][0] * rel[0] + s.Jinv[0][1] * rel[1],
-                                      s.Jinv[1][0] * rel[0] + s.Jinv[1][1] * rel[1]};
-                M2.eval(xl, &phl[(size_t)k * b]);
+            const SEl& s = el[f.left];
+            for (int k = 0; k < nq; ++k) {
+                double phys[3];
+                for (int d = 0; d < N; ++d) {
+                    double acc = 0;
+                    for (int j = 1; j < N; ++j) acc += (P_(f.v[j], d) - P_(f.v[0], d)) * qx[(size_t)k * (N - 1) + j - 1];
+                    phys[d] = P_(f.v[0], d) + acc;
+                }
+                double rel[3], xl[3];
+                for (int d = 0; d < N; ++d) rel[d] = phys[d] - s.p[0][d];
+                for (int i = 0; i < N; ++i) {
+                    double acc = 0;
+                    for (int d = 0; d < N; ++d) acc += s.Jinv[i][d] * rel[d];
+                    xl[i] = acc;
+                }
+                MS.eval(xl, &phl[(size_t)k * b]);
             }
             for (int a = 0; a < b; ++a)
-                for (int k = 0; k < MGLDG_QF; ++k)
-                    Lm[(size_t)a * MGLDG_QF + k] = phl[(size_t)k * b + a] * (kQuadWeights[k] * f.area);
+                for (int k = 0; k < nq; ++k) Lm[(size_t)a * nq + k] = phl[(size_t)k * b + a] * (qw[k] * f.area);
             for (int a = 0; a < b; ++a)
                 for (int c = 0; c < b; ++c) {
                     double sum = 0;
-                    for (int k = 0; k < MGLDG_QF; ++k) sum += Lm[(size_t)a * MGLDG_QF + k] * phl[(size_t)k * b + c];
+                    for (int k = 0; k < nq; ++k) sum += Lm[(size_t)a * nq + k] * phl[(size_t)k * b + c];
                     LL[(size_t)a * b + c] = sum;
                 }
-            const double jac = M2.volume / s.vol;
-            for (size_t k = 0; k < bsz; ++k) Minv[k] = M2.invmass[k] * jac;
-            for (int d = 0; d < 2; ++d) {
-                double* G = &bvals[((size_t)3 * q + d) * bsz];
+            const double jac = MS.volume / s.vol;
+            for (size_t k = 0; k < bsz; ++k) Minv[k] = MS.invmass[k] * jac;
+            for (int d = 0; d < N; ++d) {
+                double* G = &bvals[((size_t)nkb * q + d) * bsz];
                 const double sc = -f.n[d];
                 for (int r = 0; r < b; ++r)
                     for (int c = 0; c < b; ++c) {
@@ -596,7 +724,7 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int np, const double* pts, int nt
                         G[(size_t)r * b + c] = sum;
                     }
             }
-            double* T = &bvals[((size_t)3 * q + 2) * bsz];
+            double* T = &bvals[((size_t)nkb * q + N) * bsz];
             for (size_t k = 0; k < bsz; ++k) T[k] = tauD * LL[k];
         }
     }
@@ -606,27 +734,27 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int np, const double* pts, int nt
         int row, col;
         int64_t seq, contrib;
     };
-    std::vector<Tr> tm, tg[2], tt;
+    std::vector<Tr> tm, tg[3], tt;
     int64_t seq = 0;
     for (int e = 0; e < nt; ++e) tm.push_back({e, e, seq++, c_elem + e});
-    for (int d = 0; d < 2; ++d)
+    for (int d = 0; d < N; ++d)
         for (int e = 0; e < nt; ++e) tg[d].push_back({e, e, seq++, c_elem + (int64_t)(1 + d) * nt + e});
     for (int k = 0; k < nf; ++k) {
         const HF& f = faces[k];
         if (f.right >= 0) {
-            const int64_t base = c_face + (int64_t)8 * slot[k];
-            for (int d = 0; d < 2; ++d) {
+            const int64_t base = c_face + (int64_t)nkf * slot[k];
+            for (int d = 0; d < N; ++d) {
                 tg[d].push_back({f.right, f.right, seq++, base + 2 * d});
                 tg[d].push_back({f.right, f.left, seq++, base + 2 * d + 1});
             }
-            tt.push_back({f.right, f.right, seq++, base + 4});
-            tt.push_back({f.left, f.left, seq++, base + 5});
-            tt.push_back({f.right, f.left, seq++, base + 6});
-            tt.push_back({f.left, f.right, seq++, base + 7});
+            tt.push_back({f.right, f.right, seq++, base + 2 * N});
+            tt.push_back({f.left, f.left, seq++, base + 2 * N + 1});
+            tt.push_back({f.right, f.left, seq++, base + 2 * N + 2});
+            tt.push_back({f.left, f.right, seq++, base + 2 * N + 3});
         } else {
-            const int64_t base = c_bnd + (int64_t)3 * slot[k];
-            for (int d = 0; d < 2; ++d) tg[d].push_back({f.left, f.left, seq++, base + d});
-            tt.push_back({f.left, f.left, seq++, base + 2});
+            const int64_t base = c_bnd + (int64_t)nkb * slot[k];
+            for (int d = 0; d < N; ++d) tg[d].push_back({f.left, f.left, seq++, base + d});
+            tt.push_back({f.left, f.left, seq++, base + N});
         }
     }
     auto assemble = [&](std::vector<Tr>& v) {
@@ -650,8 +778,10 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int np, const double* pts, int nt
         }
         return As;
     };
-    MG_REQUIRE(ncontrib < (int64_t)1 << 31, MGLDG_ERR_UNSUPPORTED, "mesh too large for the contribution index");
-    const Assembly AM = assemble(tm), AG0 = assemble(tg[0]), AG1 = assemble(tg[1]), AT = assemble(tt);
+    const Assembly AM = assemble(tm);
+    std::vector<Assembly> AG;
+    for (int d = 0; d < N; ++d) AG.push_back(assemble(tg[d]));
+    const Assembly AT = assemble(tt);
 
     // ---- GPU: contributions, then the operators ----
     mgldg_problem* pr = new mgldg_problem();
@@ -661,20 +791,25 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int np, const double* pts, int nt
     pr->ne = nt;
     pr->n = 0;
     pr->simplex = true;
+    pr->sdim = N;
     pr->nfaces = nf;
     pr->nbfaces = nb;
     double *d_contrib = nullptr, *d_geom = nullptr, *d_ref = nullptr;
     FaceDev* d_faces = nullptr;
-    mgldg_bsr *M = nullptr, *G0 = nullptr, *G1 = nullptr, *Tm = nullptr;
+    mgldg_bsr* M = nullptr;
+    std::vector<mgldg_bsr*> Gs;
+    mgldg_bsr* Tm = nullptr;
     try {
-        std::vector<double> geom((size_t)nt * 11);
+        std::vector<double> geom((size_t)nt * kGeom, 0.0);
         for (int e = 0; e < nt; ++e) {
-            double* g = &geom[(size_t)e * 11];
-            g[0] = el[e].p[0][0];
-            g[1] = el[e].p[0][1];
-            g[2] = el[e].J[0][0]; g[3] = el[e].J[0][1]; g[4] = el[e].J[1][0]; g[5] = el[e].J[1][1];
-            g[6] = el[e].Jinv[0][0]; g[7] = el[e].Jinv[0][1]; g[8] = el[e].Jinv[1][0]; g[9] = el[e].Jinv[1][1];
-            g[10] = el[e].vol;
+            double* g = &geom[(size_t)e * kGeom];
+            for (int d = 0; d < N; ++d) g[d] = el[e].p[0][d];
+            for (int d = 0; d < 3; ++d)
+                for (int i = 0; i < 3; ++i) {
+                    g[3 + d * 3 + i] = el[e].J[d][i];
+                    g[12 + d * 3 + i] = el[e].Jinv[d][i];
+                }
+            g[21] = el[e].vol;
         }
         std::vector<FaceDev> fd(nfi);
         for (int q = 0; q < nfi; ++q) {
@@ -682,23 +817,20 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int np, const double* pts, int nt
             FaceDev& D = fd[q];
             D.left = f.left;
             D.right = f.right;
-            D.n0 = f.n[0];
-            D.n1 = f.n[1];
-            D.area = f.area;
+            for (int d = 0; d < 3; ++d) D.n[d] = d < N ? f.n[d] : 0.0;
+            D.jac = f.area / MF.volume;   // Face::mass (mesh.h:100-104)
             D.volR = el[f.right].vol;
-            for (int a = 0; a < 6; ++a) {
+            for (int a = 0; a < 10; ++a) {
                 D.sl[a] = a < P1 ? f.sl[a] : -1;
                 D.sr[a] = a < P1 ? f.sr[a] : -1;
             }
         }
-        // reference tables: Mref | D0 | D1 | Minv | M1 | nodes
+        // reference tables: Mref | D_0..D_{N-1} | Minv | Mface
         std::vector<double> ref;
-        ref.insert(ref.end(), M2.mass.begin(), M2.mass.end());
-        ref.insert(ref.end(), M2.diff[0].begin(), M2.diff[0].end());
-        ref.insert(ref.end(), M2.diff[1].begin(), M2.diff[1].end());
-        ref.insert(ref.end(), M2.invmass.begin(), M2.invmass.end());
-        ref.insert(ref.end(), M1.mass.begin(), M1.mass.end());
-        ref.insert(ref.end(), M2.nodes.begin(), M2.nodes.end());
+        ref.insert(ref.end(), MS.mass.begin(), MS.mass.end());
+        for (int d = 0; d < N; ++d) ref.insert(ref.end(), MS.diff[d].begin(), MS.diff[d].end());
+        ref.insert(ref.end(), MS.invmass.begin(), MS.invmass.end());
+        ref.insert(ref.end(), MF.mass.begin(), MF.mass.end());
         d_geom = dalloc<double>(geom.size());
         d_ref = dalloc<double>(ref.size());
         d_faces = dalloc<FaceDev>(std::max(1, nfi));
@@ -708,46 +840,46 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int np, const double* pts, int nt
         if (nfi) upload(ctx, d_faces, fd.data(), fd.size());
         if (nb) upload(ctx, d_contrib + (size_t)c_bnd * bsz, bvals.data(), bvals.size());
         const double* dM = d_ref;
-        const double* dD0 = d_ref + bsz;
-        const double* dD1 = d_ref + 2 * bsz;
-        const double* dMinv = d_ref + 3 * bsz;
-        const double* dM1 = d_ref + 4 * bsz;
+        const double* dD = d_ref + bsz;
+        const double* dMinv = d_ref + (size_t)(1 + N) * bsz;
+        const double* dMf = d_ref + (size_t)(2 + N) * bsz;
         {
             const int64_t tot = (int64_t)nt * bsz;
             const int g = (int)std::max<int64_t>(1, std::min<int64_t>((tot + 255) / 256, ctx->sm_count * 32));
             Launch L(ctx, MGLDG_K_SETUP);
-            k_simplex_elem<<<g, 256, 0, ctx->stream>>>(nt, b, d_geom, dM, dD0, dD1, M2.volume, d_contrib);
+            k_simplex_elem<<<g, 256, 0, ctx->stream>>>(nt, N, b, d_geom, dM, dD, MS.volume, d_contrib);
         }
         check_launch();
         if (nfi) {
-            const int64_t tot = (int64_t)nfi * 8 * bsz;
+            const int64_t tot = (int64_t)nfi * nkf * bsz;
             const int g = (int)std::max<int64_t>(1, std::min<int64_t>((tot + 255) / 256, ctx->sm_count * 32));
             Launch L(ctx, MGLDG_K_SETUP);
-            k_simplex_face<<<g, 256, 0, ctx->stream>>>(nfi, b, P1, d_faces, dM1, dMinv, M2.volume, tau0,
+            k_simplex_face<<<g, 256, 0, ctx->stream>>>(nfi, N, b, P1, d_faces, dMf, dMinv, MS.volume, tau0,
                                                        d_contrib + (size_t)c_face * bsz);
         }
         check_launch();
         M = realize(ctx, AM, nt, b, d_contrib);
-        G0 = realize(ctx, AG0, nt, b, d_contrib);
-        G1 = realize(ctx, AG1, nt, b, d_contrib);
+        for (int d = 0; d < N; ++d) Gs.push_back(realize(ctx, AG[d], nt, b, d_contrib));
         Tm = realize(ctx, AT, nt, b, d_contrib);
         pr->ops = new mgldg_ops();
         pr->ops->ctx = ctx;
-        pr->ops->ndim = 2;
+        pr->ops->ndim = N;
         pr->ops->M = M; M = nullptr;
-        pr->ops->G[0] = G0; G0 = nullptr;
-        pr->ops->G[1] = G1; G1 = nullptr;
+        for (int d = 0; d < N; ++d) {
+            pr->ops->G[d] = Gs[d];
+            Gs[d] = nullptr;
+        }
         pr->ops->T = Tm; Tm = nullptr;
         construct_laplacian(ctx, pr->ops);
         // geometry for right-hand sides and dumps
         pr->sgeom = geom;
-        pr->snodes = M2.nodes;
+        pr->snodes = MS.nodes;
         pr->d_geom = d_geom; d_geom = nullptr;
-        pr->d_nodes = dalloc<double>(M2.nodes.size());
-        upload(ctx, pr->d_nodes, M2.nodes.data(), M2.nodes.size());
+        pr->d_nodes = dalloc<double>(MS.nodes.size());
+        upload(ctx, pr->d_nodes, MS.nodes.data(), MS.nodes.size());
         pr->d_Mref = dalloc<double>(bsz);
-        upload(ctx, pr->d_Mref, M2.mass.data(), bsz);
-        pr->svref = M2.volume;
+        upload(ctx, pr->d_Mref, MS.mass.data(), bsz);
+        pr->svref = MS.volume;
 
         // ---- agglomeration hierarchy (interpolationhierarchy.h:89-210) ----
         Graph adj(nt);
@@ -759,19 +891,35 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int np, const double* pts, int nt
         for (auto& a : adj) std::sort(a.begin(), a.end());
         std::vector<SBox> box(nt), fbox;
         for (int e = 0; e < nt; ++e)
-            for (int d = 0; d < 2; ++d) {
+            for (int d = 0; d < N; ++d) {
                 box[e].lo[d] = box[e].hi[d] = el[e].p[0][d];
-                for (int j = 1; j < 3; ++j) {
+                for (int j = 1; j < nv; ++j) {
                     box[e].lo[d] = std::min(box[e].lo[d], el[e].p[j][d]);
                     box[e].hi[d] = std::max(box[e].hi[d], el[e].p[j][d]);
                 }
             }
         const Ref2 CR(P);
-        const int cb = P * P;
+        const int cb = N == 2 ? P * P : P * P * P;
+        // tensor Lagrange basis of the box at x (Cartesian LagrangePoly<P>,
+        // last index fastest)
+        auto lagrangeN = [&](const double* x, double* out) {
+            double l[3][8];
+            for (int d = 0; d < N; ++d) CR.lagrange1(x[d], l[d]);
+            int k = 0;
+            for (int i0 = 0; i0 < P; ++i0)
+                for (int i1 = 0; i1 < P; ++i1)
+                    for (int i2 = 0; i2 < (N == 3 ? P : 1); ++i2) {
+                        double v = 1;
+                        v *= l[0][i0];
+                        v *= l[1][i1];
+                        if (N == 3) v *= l[2][i2];
+                        out[k++] = v;
+                    }
+        };
         int nfine = nt;
         for (int lev = 0; lev < agg_levels && nfine > 1; ++lev) {
             int nc = 0;
-            std::vector<int> agg = greedy_agglomerate(nfine, adj, agg_seed + (uint64_t)lev, &nc);
+            std::vector<int> agg = greedy_agglomerate(nfine, adj, agg_seed + (uint64_t)lev, N, &nc);
             if (nc >= nfine) break;
             const std::vector<SBox>& src = lev == 0 ? box : fbox;
             std::vector<SBox> cbox(nc);
@@ -785,44 +933,52 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int np, const double* pts, int nt
                     seen[a] = 1;
                     continue;
                 }
-                for (int d = 0; d < 2; ++d) {
+                for (int d = 0; d < N; ++d) {
                     cbox[a].lo[d] = std::min(cbox[a].lo[d], src[u].lo[d]);
                     cbox[a].hi[d] = std::max(cbox[a].hi[d], src[u].hi[d]);
                 }
             }
             const int br = lev == 0 ? b : cb;
-            std::vector<double> vals((size_t)nfine * br * cb);
+            std::vector<double> vals((size_t)nfine * br * cb, 0.0);
             for (int u = 0; u < nfine; ++u) {
                 const int a = agg[u];
                 const SBox& B = cbox[a];
-                const double w[2] = {B.hi[0] - B.lo[0], B.hi[1] - B.lo[1]};
+                double w[3];
+                for (int d = 0; d < N; ++d) w[d] = B.hi[d] - B.lo[d];
                 double* E = &vals[(size_t)u * br * cb];
                 if (lev == 0) {
-                    double rp[3][2];
-                    for (int j = 0; j < 3; ++j)
-                        for (int d = 0; d < 2; ++d) rp[j][d] = (el[u].p[j][d] - B.lo[d]) / w[d];
+                    // the fine simplex mapped into the box, the box's tensor
+                    // basis at its nodes
+                    double rp[4][3];
+                    for (int j = 0; j < nv; ++j)
+                        for (int d = 0; d < N; ++d) rp[j][d] = (el[u].p[j][d] - B.lo[d]) / w[d];
                     for (int i = 0; i < b; ++i) {
-                        double x[2];
-                        for (int d = 0; d < 2; ++d)
-                            x[d] = rp[0][d] + ((rp[1][d] - rp[0][d]) * M2.nodes[2 * i] +
-                                               (rp[2][d] - rp[0][d]) * M2.nodes[2 * i + 1]);
-                        CR.lagrange2(x, E + (size_t)i * cb);
+                        double x[3];
+                        for (int d = 0; d < N; ++d) {
+                            double acc = (rp[1][d] - rp[0][d]) * MS.nodes[(size_t)N * i];
+                            for (int j = 1; j < N; ++j) acc += (rp[j + 1][d] - rp[0][d]) * MS.nodes[(size_t)N * i + j];
+                            x[d] = rp[0][d] + acc;
+                        }
+                        lagrangeN(x, E + (size_t)i * cb);
                     }
                 } else if (cnt[a] == 1) {
                     for (int i = 0; i < cb; ++i) E[(size_t)i * cb + i] = 1.0;
                 } else {
                     const SBox& F = src[u];
-                    double rlo[2], rhi[2];
-                    for (int d = 0; d < 2; ++d) {
+                    double rlo[3], rhi[3];
+                    for (int d = 0; d < N; ++d) {
                         rlo[d] = (F.lo[d] - B.lo[d]) / w[d];
                         rhi[d] = (F.hi[d] - B.lo[d]) / w[d];
                     }
+                    int row = 0;
                     for (int i0 = 0; i0 < P; ++i0)
-                        for (int i1 = 0; i1 < P; ++i1) {
-                            const double x[2] = {rlo[0] + (rhi[0] - rlo[0]) * CR.nodes[i0],
-                                                 rlo[1] + (rhi[1] - rlo[1]) * CR.nodes[i1]};
-                            CR.lagrange2(x, E + (size_t)(i0 * P + i1) * cb);
-                        }
+                        for (int i1 = 0; i1 < P; ++i1)
+                            for (int i2 = 0; i2 < (N == 3 ? P : 1); ++i2) {
+                                const int id[3] = {i0, i1, i2};
+                                double x[3];
+                                for (int d = 0; d < N; ++d) x[d] = rlo[d] + (rhi[d] - rlo[d]) * CR.nodes[id[d]];
+                                lagrangeN(x, E + (size_t)(row++) * cb);
+                            }
                 }
             }
             pr->T.push_back(host_bsr(ctx, nfine, nc, br, cb, agg, vals));
@@ -838,7 +994,9 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int np, const double* pts, int nt
         dfree(d_geom);
         dfree(d_ref);
         dfree(d_faces);
-        delete M; delete G0; delete G1; delete Tm;
+        delete M;
+        for (auto* g : Gs) delete g;
+        delete Tm;
         delete pr;
         throw;
     }
@@ -849,12 +1007,12 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int np, const double* pts, int nt
 }
 
 void simplex_rhs_dev(mgldg_ctx* ctx, const mgldg_problem* pr, uint64_t seed, double* b) {
-    const GaussDevS g = gaussian_disk(seed);
+    const GaussDevS g = gaussian_ball(seed, pr->sdim);
     const int grid = std::max(1, std::min(pr->ne, ctx->sm_count * 32));
     {
         Launch L(ctx, MGLDG_K_SETUP);
-        k_rhs_simplex<<<grid, 64, pr->b * sizeof(double), ctx->stream>>>(pr->ne, pr->b, pr->d_geom, pr->d_nodes,
-                                                                         pr->d_Mref, pr->svref, g, b);
+        k_rhs_simplex<<<grid, 64, pr->b * sizeof(double), ctx->stream>>>(pr->ne, pr->sdim, pr->b, pr->d_geom,
+                                                                         pr->d_nodes, pr->d_Mref, pr->svref, g, b);
     }
     check_launch();
 }
@@ -912,6 +1070,51 @@ static void disk_mesh(double h, std::vector<double>& p, std::vector<int>& t) {
             }
         }
     }
+}
+
+// Ball mesher (no reference counterpart): the cube [-1,1]^3 on an n^3 grid
+// (n = ceil(1.4/h)), every cube cut into the six tetrahedra of its Kuhn
+// triangulation (conforming across cubes), vertices mapped onto the ball by
+// x -> x |x|_inf / |x|_2.  Positively oriented tetrahedra.
+static void ball_mesh(double h, std::vector<double>& p, std::vector<int>& t) {
+    MG_REQUIRE(h > 0 && h <= 2, MGLDG_ERR_ARG, "mesh size must be in (0, 2]");
+    const int n = std::max(1, (int)std::ceil(1.4 / h - 1e-12));
+    MG_REQUIRE(n <= 256, MGLDG_ERR_ARG, "mesh size too small");
+    const int m = n + 1;
+    p.clear();
+    t.clear();
+    for (int i = 0; i < m; ++i)
+        for (int j = 0; j < m; ++j)
+            for (int k = 0; k < m; ++k) {
+                double x[3] = {-1 + 2.0 * i / n, -1 + 2.0 * j / n, -1 + 2.0 * k / n};
+                const double inf = std::max(std::fabs(x[0]), std::max(std::fabs(x[1]), std::fabs(x[2])));
+                const double two = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+                const double s = two > 0 ? inf / two : 0.0;
+                for (int d = 0; d < 3; ++d) p.push_back(x[d] * s);
+            }
+    auto vid = [&](int i, int j, int k) { return (i * m + j) * m + k; };
+    const int perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j)
+            for (int k = 0; k < n; ++k)
+                for (auto& pm : perm) {
+                    int c[3] = {i, j, k};
+                    int v[4];
+                    v[0] = vid(c[0], c[1], c[2]);
+                    for (int s = 0; s < 3; ++s) {
+                        c[pm[s]] += 1;
+                        v[s + 1] = vid(c[0], c[1], c[2]);
+                    }
+                    // orient positively
+                    double a[3][3];
+                    for (int s = 0; s < 3; ++s)
+                        for (int d = 0; d < 3; ++d) a[s][d] = p[3 * v[s + 1] + d] - p[3 * v[0] + d];
+                    const double det = a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) -
+                                       a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]) +
+                                       a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
+                    if (det < 0) std::swap(v[2], v[3]);
+                    for (int s = 0; s < 4; ++s) t.push_back(v[s]);
+                }
 }
 
 }  // namespace mg
@@ -988,17 +1191,23 @@ extern "C" int mgldg_mesh_read(const char* path, int* np, int* nt, double* p, in
     return MGLDG_OK;
 }
 
-extern "C" int mgldg_simplex_problem_create(mgldg_ctx* ctx, int np, const double* p, int nt, const int* t, int P,
-                                            double tau0, double tauD, int agg_levels, uint64_t agg_seed,
-                                            mgldg_problem** out) {
+extern "C" int mgldg_simplex_problem_create_nd(mgldg_ctx* ctx, int N, int np, const double* p, int nt, const int* t,
+                                               int P, double tau0, double tauD, int agg_levels, uint64_t agg_seed,
+                                               mgldg_problem** out) {
     MG_API_BEGIN(ctx)
     MG_REQUIRE(out != nullptr && agg_levels >= 0, MGLDG_ERR_ARG, "bad arguments");
     *out = nullptr;
     std::vector<std::vector<int>> parts;
-    mgldg_problem* pr = simplex_problem(ctx, np, p, nt, t, P, tau0, tauD, agg_levels, agg_seed, &parts);
+    mgldg_problem* pr = simplex_problem(ctx, N, np, p, nt, t, P, tau0, tauD, agg_levels, agg_seed, &parts);
     pr->partitions = std::move(parts);
     *out = pr;
     MG_API_END
+}
+
+extern "C" int mgldg_simplex_problem_create(mgldg_ctx* ctx, int np, const double* p, int nt, const int* t, int P,
+                                            double tau0, double tauD, int agg_levels, uint64_t agg_seed,
+                                            mgldg_problem** out) {
+    return mgldg_simplex_problem_create_nd(ctx, 2, np, p, nt, t, P, tau0, tauD, agg_levels, agg_seed, out);
 }
 
 extern "C" int mgldg_problem_partition(const mgldg_problem* pr, int l, int* n, int* agg) {
@@ -1006,6 +1215,20 @@ extern "C" int mgldg_problem_partition(const mgldg_problem* pr, int l, int* n, i
     const std::vector<int>& a = pr->partitions[l];
     *n = (int)a.size();
     if (agg) std::copy(a.begin(), a.end(), agg);
+    return MGLDG_OK;
+}
+
+extern "C" int mgldg_simplex_master_nd(int N, int P, double* mass, double* diff, double* nodes) {
+    if (N < 1 || N > 3 || P < 1 || P > 6 || !mass || !nodes) return MGLDG_ERR_ARG;
+    try {
+        const SMaster m(N, P);
+        std::copy(m.mass.begin(), m.mass.end(), mass);
+        if (diff)
+            for (int d = 0; d < N; ++d) std::copy(m.diff[d].begin(), m.diff[d].end(), diff + (size_t)d * m.b * m.b);
+        std::copy(m.nodes.begin(), m.nodes.end(), nodes);
+    } catch (const Error& e) {
+        return e.code;
+    }
     return MGLDG_OK;
 }
 
@@ -1019,6 +1242,24 @@ extern "C" int mgldg_simplex_master(int N, int P, double* mass, double* diff0, d
         std::copy(m.nodes.begin(), m.nodes.end(), nodes);
     } catch (const Error& e) {
         return e.code;
+    }
+    return MGLDG_OK;
+}
+
+extern "C" int mgldg_ball_mesh(double h, int* np, int* nt, double* p, int* t) {
+    if (!np || !nt) return MGLDG_ERR_ARG;
+    try {
+        std::vector<double> pv;
+        std::vector<int> tv;
+        ball_mesh(h, pv, tv);
+        *np = (int)pv.size() / 3;
+        *nt = (int)tv.size() / 4;
+        if (p) std::copy(pv.begin(), pv.end(), p);
+        if (t) std::copy(tv.begin(), tv.end(), t);
+    } catch (const Error& e) {
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        return MGLDG_ERR_NOMEM;
     }
     return MGLDG_OK;
 }

@@ -366,10 +366,12 @@ void gs_sweep(mgldg_ctx* ctx, const mgldg_bsr* A, const T* vals, const T* Dinv, 
         case 3: launch_gs<T, 3>(ctx, A, vals, Dinv, b, x, S, omega, reverse); return;
         case 4: launch_gs<T, 4>(ctx, A, vals, Dinv, b, x, S, omega, reverse); return;
         case 6: launch_gs<T, 6>(ctx, A, vals, Dinv, b, x, S, omega, reverse); return;
+        case 8: launch_gs<T, 8>(ctx, A, vals, Dinv, b, x, S, omega, reverse); return;
         case 9: launch_gs<T, 9>(ctx, A, vals, Dinv, b, x, S, omega, reverse); return;
         case 10: launch_gs<T, 10>(ctx, A, vals, Dinv, b, x, S, omega, reverse); return;
         case 16: launch_gs<T, 16>(ctx, A, vals, Dinv, b, x, S, omega, reverse); return;
         case 25: launch_gs<T, 25>(ctx, A, vals, Dinv, b, x, S, omega, reverse); return;
+        case 27: launch_gs<T, 27>(ctx, A, vals, Dinv, b, x, S, omega, reverse); return;
     }
     throw Error(MGLDG_ERR_UNSUPPORTED, "Gauss-Seidel: unsupported block size");
 }
@@ -403,10 +405,12 @@ void jacobi_sweep(mgldg_ctx* ctx, const mgldg_bsr* A, const T* vals, const T* Di
         case 3: launch_jacobi<T, 3>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
         case 4: launch_jacobi<T, 4>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
         case 6: launch_jacobi<T, 6>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
+        case 8: launch_jacobi<T, 8>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
         case 9: launch_jacobi<T, 9>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
         case 10: launch_jacobi<T, 10>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
         case 16: launch_jacobi<T, 16>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
         case 25: launch_jacobi<T, 25>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
+        case 27: launch_jacobi<T, 27>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
     }
     throw Error(MGLDG_ERR_UNSUPPORTED, "Jacobi: unsupported block size");
 }

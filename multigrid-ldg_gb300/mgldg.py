@@ -43,6 +43,7 @@ EXPORTS = [
     "mgldg_quadtree_layer", "mgldg_h_points", "mgldg_seeded_points", "mgldg_quadtree_problem_create",
     "mgldg_problem_mesh_info", "mgldg_mesh_read", "mgldg_disk_mesh", "mgldg_simplex_problem_create",
     "mgldg_problem_partition", "mgldg_simplex_master", "mgldg_pcg_segmented_dev",
+    "mgldg_simplex_problem_create_nd", "mgldg_ball_mesh", "mgldg_simplex_master_nd",
 ]
 
 
@@ -164,6 +165,10 @@ def lib():
                                                    C.c_int, C.c_uint64, pvp]
         L.mgldg_problem_partition.argtypes = [vp, C.c_int, ip, vp]
         L.mgldg_simplex_master.argtypes = [C.c_int, C.c_int, _dp, vp, vp, _dp]
+        L.mgldg_simplex_problem_create_nd.argtypes = [vp, C.c_int, C.c_int, _dp, C.c_int, _ip, C.c_int, C.c_double,
+                                                      C.c_double, C.c_int, C.c_uint64, pvp]
+        L.mgldg_ball_mesh.argtypes = [C.c_double, ip, ip, vp, vp]
+        L.mgldg_simplex_master_nd.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp]
         L.mgldg_pcg_segmented_dev.argtypes = [vp, vp, vp, C.c_int, C.POINTER(C.c_int64), vp, vp, C.c_double,
                                               C.c_int, _ip, _dp]
         _lib = L
@@ -565,13 +570,13 @@ class Quadtree:
             self.h = None
 
 
-def _two_call(fn, *head):
+def _two_call(fn, *head, N=2):
     np_, nt = C.c_int(), C.c_int()
     rc = fn(*head, C.byref(np_), C.byref(nt), None, None)
     if rc:
         raise MgldgError(rc, "mesh")
-    p = np.zeros((np_.value, 2))
-    t = np.zeros((nt.value, 3), np.int32)
+    p = np.zeros((np_.value, N))
+    t = np.zeros((nt.value, N + 1), np.int32)
     rc = fn(*head, C.byref(np_), C.byref(nt), p.ctypes.data_as(C.c_void_p), t.ctypes.data_as(C.c_void_p))
     if rc:
         raise MgldgError(rc, "mesh")
@@ -583,13 +588,18 @@ def disk_mesh(h):
     return _two_call(lib().mgldg_disk_mesh, C.c_double(h))
 
 
+def ball_mesh(h):
+    """Tetrahedra of the unit ball (Kuhn-split cube grid mapped onto the ball): (points[np,3], tets[nt,4])."""
+    return _two_call(lib().mgldg_ball_mesh, C.c_double(h), N=3)
+
+
 def read_mesh(path):
     """The reference's .mesh wireframe: (points[np,2], triangles[nt,3], 0-based)."""
     return _two_call(lib().mgldg_mesh_read, str(path).encode())
 
 
 def mesh_union(meshes):
-    """Disjoint union of triangle meshes: (points, triangles, element offsets[len+1])."""
+    """Disjoint union of simplex meshes: (points, simplices, element offsets[len+1])."""
     ps, ts, off, nv, ne = [], [], [0], 0, 0
     for p, t in meshes:
         ps.append(np.asarray(p, np.float64))
@@ -621,12 +631,12 @@ def pcg_segmented(ctx, A, b, seg_offsets, precon, x=None, tol=1e-8, maxit=200):
 
 
 def simplex_master(N, P):
-    b = P if N == 1 else P * (P + 1) // 2
-    mass, d0, d1, nodes = np.zeros(b * b), np.zeros(b * b), np.zeros(b * b), np.zeros(b * N)
-    rc = lib().mgldg_simplex_master(N, P, mass, d0.ctypes.data_as(C.c_void_p), d1.ctypes.data_as(C.c_void_p), nodes)
+    b = {1: P, 2: P * (P + 1) // 2, 3: P * (P + 1) * (P + 2) // 6}[N]
+    mass, diff, nodes = np.zeros(b * b), np.zeros(N * b * b), np.zeros(b * N)
+    rc = lib().mgldg_simplex_master_nd(N, P, mass, diff, nodes)
     if rc:
         raise MgldgError(rc, "simplex_master")
-    return mass.reshape(b, b), [d0.reshape(b, b), d1.reshape(b, b)][:N], nodes.reshape(b, N)
+    return mass.reshape(b, b), list(diff.reshape(N, b, b)), nodes.reshape(b, N)
 
 
 class CartesianProblem:
@@ -638,11 +648,12 @@ class CartesianProblem:
         h = C.c_void_p()
         if mesh is not None:
             pts, tris = mesh
+            N = np.asarray(pts).shape[1]
             pts = np.ascontiguousarray(pts, np.float64).ravel()
             tris = np.ascontiguousarray(tris, np.int32).ravel()
-            ctx.check(lib().mgldg_simplex_problem_create(ctx.h, len(pts) // 2, pts, len(tris) // 3, tris, P,
-                                                         float(tau0), float(tauD), agg_levels, agg_seed,
-                                                         C.byref(h)), "simplex_problem_create")
+            ctx.check(lib().mgldg_simplex_problem_create_nd(ctx.h, N, len(pts) // N, pts, len(tris) // (N + 1), tris,
+                                                            P, float(tau0), float(tauD), agg_levels, agg_seed,
+                                                            C.byref(h)), "simplex_problem_create")
         elif quadtree is None:
             tau0 = float(n) if tau0 is None else tau0
             tauD = float(n) if tauD is None else tauD

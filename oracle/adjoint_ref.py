@@ -28,9 +28,10 @@ def to_scipy(csr):
 
 
 def operators(pr):
-    """(M, [G0, G1], T) of an oracle Problem as scipy matrices, plus M's blocks."""
+    """(M, [G0, G1(, G2)], T) of an oracle Problem as scipy matrices, plus M's blocks."""
     Mc = pr.op(O.OP_M)
-    return to_scipy(Mc), [to_scipy(pr.op(O.OP_G0)), to_scipy(pr.op(O.OP_G1))], to_scipy(pr.op(O.OP_T)), Mc
+    ids = [O.OP_G0, O.OP_G1] + ([O.OP_G2] if getattr(pr, "dim", 2) == 3 else [])
+    return to_scipy(Mc), [to_scipy(pr.op(w)) for w in ids], to_scipy(pr.op(O.OP_T)), Mc
 
 
 def kappa_laplacian(pr, kappa):
@@ -86,3 +87,14 @@ def smooth_field(n, seed, corr=0.2, sigma=0.5, nfeat=64):
         x, y = (ix + 0.5) / n, (iy + 0.5) / n
         kappa[e] = np.exp(a @ np.cos(w @ np.array([x, y]) + ph))
     return kappa
+
+
+def field_at(X, seed, corr=0.2, sigma=0.5, nfeat=64):
+    """log-normal diffusivity exp(g(x)) at points X (n x dim): random Fourier
+    features of a Gaussian covariance with length `corr` and deviation sigma."""
+    X = np.asarray(X, np.float64)
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal((nfeat, X.shape[1])) / corr
+    ph = rng.uniform(0, 2 * np.pi, nfeat)
+    a = rng.standard_normal(nfeat) * sigma * np.sqrt(2.0 / nfeat)
+    return np.exp(np.cos(X @ w.T + ph) @ a)

@@ -879,13 +879,14 @@ struct Mesh {
 // ---------------------------------------------------------- LDG operators --
 // LDGOperators<N,P> (ldgpoisson.h:15-53)
 struct Ops {
-    SBM M, G[2], T, A;
+    SBM M, G[3], T, A;
+    int ndim = NDIM;   // 3 for tetrahedral meshes
     std::vector<LDLT> Minv;
     bool has_MGT = false;
     // construct_laplacian (ldgpoisson.h:34-52): A = T + sum_d G_d^T M G_d
     void construct_laplacian() {
         A = T;
-        for (int d = 0; d < NDIM; ++d) {
+        for (int d = 0; d < ndim; ++d) {
             for (int k = 0; k < M.blockRows(); ++k) {
                 const auto& cols = G[d].colsInRow(k);
                 for (int i : cols) {
@@ -915,7 +916,8 @@ struct Problem {
     bool simplex = false;
     int s_ne = 0, s_nf = 0, s_nb = 0;
     std::vector<std::vector<int>> agg;   // per agglomeration level: aggregate of each finer element
-    std::vector<double> s_xy;            // node coordinates (x, y) in DOF order
+    std::vector<double> s_xy;            // node coordinates (s_dim per DOF) in DOF order
+    int s_dim = 2;
 };
 
 // LDGPoisson<N,P>::discretize (ldgpoisson.tpp:14-24) and its parts
@@ -1275,7 +1277,8 @@ struct MG {
             }
             for (int i = 0; i < o.M.blockRows(); ++i) o.Minv.emplace_back(o.M.get(i, i));
             SBM temp1, temp2;
-            for (int d = 0; d < NDIM; ++d) {
+            o.ndim = f.ndim;
+            for (int d = 0; d < f.ndim; ++d) {
                 multiply_mm(f.G[d], T, temp1);
                 multiply_mm(f.M, temp1, temp2);
                 multiply_mm_t(T, temp2, o.G[d]);
@@ -1462,6 +1465,7 @@ static const SBM& op_of(const Ops& o, int which) {
         case 2: return o.G[1];
         case 3: return o.T;
         case 4: return o.A;
+        case 5: if (o.ndim > 2) return o.G[2]; break;
     }
     throw std::invalid_argument("bad operator id");
 }
@@ -1778,11 +1782,12 @@ int orc_problem_write_fun(const orc_problem* pr, const double* u, const char* pa
         ofs.precision(std::numeric_limits<double>::max_digits10);
         if (p.simplex) {
             // unstructured Function::write (src/unstructured/dg/function.h:159-176)
-            ofs << p.P << " " << NDIM << " " << p.s_ne << std::endl;
+            ofs << p.P << " " << p.s_dim << " " << p.s_ne << std::endl;
             for (int e = 0; e < p.s_ne; ++e) {
                 for (int i = 0; i < p.npl; ++i) {
                     size_t k = (size_t)e * p.npl + i;
-                    ofs << p.s_xy[2 * k] << " " << p.s_xy[2 * k + 1] << " " << u[k] << std::endl;
+                    for (int d = 0; d < p.s_dim; ++d) ofs << p.s_xy[k * p.s_dim + d] << " ";
+                    ofs << u[k] << std::endl;
                 }
                 ofs << std::endl;
             }

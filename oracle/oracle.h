@@ -75,6 +75,11 @@ int orc_seeded_points(uint64_t seed, int n, double* xy);
  * tensor-product coarse spaces on the aggregates' bounding boxes). */
 int orc_simplex_problem_create(int np, const double* p, int nt, const int* t, int P, double tau0, double tauD,
                                int agg_levels, uint64_t agg_seed, uint64_t rhs_seed, orc_problem** out);
+/* N = 2 (triangles, p[2*np], t[3*nt]) or 3 (tetrahedra, p[3*np], t[4*nt]) */
+int orc_simplex_problem_create_nd(int N, int np, const double* p, int nt, const int* t, int P, double tau0,
+                                  double tauD, int agg_levels, uint64_t agg_seed, uint64_t rhs_seed,
+                                  orc_problem** out);
+int orc_simplex_master_nd(int N, int P, double* mass, double* diff, double* nodes);
 /* block shape of hierarchy level l; aggregate of every finer element at agglomeration level l */
 int orc_hier_block(const orc_problem* pr, int l, int* br, int* bc);
 int orc_problem_partition(const orc_problem* pr, int l, int* agg);

@@ -21,7 +21,7 @@ TEST_CONVERGENCE, TEST_SOLUTION, TEST_GAUSSIAN = 0, 1, 2
 RELAX_JACOBI, RELAX_GS = 0, 1
 COARSE_CHOLESKY, COARSE_RELAX, COARSE_DENSE = 0, 1, 2
 RESTRICT_RAT, RESTRICT_RATRAT = 0, 1
-OP_M, OP_G0, OP_G1, OP_T, OP_A = 0, 1, 2, 3, 4
+OP_M, OP_G0, OP_G1, OP_T, OP_A, OP_G2 = 0, 1, 2, 3, 4, 5
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
@@ -87,6 +87,9 @@ def lib():
         L.orc_hier_block.argtypes = [vp, C.c_int, ip, ip]
         L.orc_problem_partition.argtypes = [vp, C.c_int, _ip]
         L.orc_simplex_master.argtypes = [C.c_int, C.c_int, _dp, vp, vp, _dp]
+        L.orc_simplex_problem_create_nd.argtypes = [C.c_int, C.c_int, _dp, C.c_int, _ip, C.c_int, C.c_double,
+                                                    C.c_double, C.c_int, C.c_uint64, C.c_uint64, pvp]
+        L.orc_simplex_master_nd.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp]
         _lib = L
     return _lib
 
@@ -112,12 +115,10 @@ def quadrature(Q):
 
 def simplex_master(N, P):
     """(mass, diff[N], nodes) of the master simplex (unstructured master.h)."""
-    npl = {1: P, 2: P * (P + 1) // 2}[N]
-    mass, d0, d1, nodes = np.zeros(npl * npl), np.zeros(npl * npl), np.zeros(npl * npl), np.zeros(npl * N)
-    _ck(lib().orc_simplex_master(N, P, mass, d0.ctypes.data_as(C.c_void_p), d1.ctypes.data_as(C.c_void_p), nodes),
-        "simplex_master")
-    diffs = [d0.reshape(npl, npl), d1.reshape(npl, npl)][:N]
-    return mass.reshape(npl, npl), diffs, nodes.reshape(npl, N)
+    npl = {1: P, 2: P * (P + 1) // 2, 3: P * (P + 1) * (P + 2) // 6}[N]
+    mass, diff, nodes = np.zeros(npl * npl), np.zeros(N * npl * npl), np.zeros(npl * N)
+    _ck(lib().orc_simplex_master_nd(N, P, mass, diff, nodes), "simplex_master")
+    return mass.reshape(npl, npl), list(diff.reshape(N, npl, npl)), nodes.reshape(npl, N)
 
 
 def seeded_points(seed, n):
@@ -220,11 +221,13 @@ class Problem:
         """Unstructured P_{P-1} LDG on a triangle mesh (see oracle.h); seed 0: f = 1."""
         self = cls.__new__(cls)
         h = C.c_void_p()
+        N = np.asarray(points).shape[1]
         p = np.ascontiguousarray(points, np.float64).ravel()
         t = np.ascontiguousarray(tris, np.int32).ravel()
-        _ck(lib().orc_simplex_problem_create(len(p) // 2, p, len(t) // 3, t, P, tau0, tauD, agg_levels, agg_seed,
-                                             seed, C.byref(h)), "simplex_problem_create")
+        _ck(lib().orc_simplex_problem_create_nd(N, len(p) // N, p, len(t) // (N + 1), t, P, tau0, tauD, agg_levels,
+                                                agg_seed, seed, C.byref(h)), "simplex_problem_create")
         self._attach(h, P)
+        self.dim = N
         return self
 
     def partition(self, l):

@@ -22,7 +22,7 @@ def _lib_or_skip():
         pytest.skip(str(e))
 
 
-@pytest.mark.parametrize("N,P", [(1, 1), (1, 3), (2, 1), (2, 2), (2, 3), (2, 4)])
+@pytest.mark.parametrize("N,P", [(1, 1), (1, 3), (2, 1), (2, 2), (2, 3), (2, 4), (3, 1), (3, 2), (3, 3)])
 def test_master_matches_oracle(N, P):
     _lib_or_skip()
     m, d, nodes = mgldg.simplex_master(N, P)
@@ -32,7 +32,7 @@ def test_master_matches_oracle(N, P):
     for a, c in zip(d, do):
         assert np.abs(a - c).max() <= 1e-14 * max(1, np.abs(c).max())
     # mass integrates 1 to the master volume; rows of diff kill constants
-    vref = 1.0 if N == 1 else 0.5
+    vref = {1: 1.0, 2: 0.5, 3: 1 / 6}[N]
     assert abs(m.sum() - vref) <= 1e-15
     for a in d:
         assert np.abs(a.sum(axis=1)).max() <= 1e-13
@@ -123,3 +123,43 @@ def test_agglomeration_covers_and_coarsens():
     # interpolation of a constant is the constant
     for T in H:
         assert np.allclose(T.matvec(np.ones(T.nbc * T.bc)), 1.0, atol=1e-12)
+
+
+def test_ball_mesh_is_a_conforming_tetrahedralisation():
+    _lib_or_skip()
+    p, t = mgldg.ball_mesh(0.3)
+    a, b, c = (p[t[:, k]] - p[t[:, 0]] for k in (1, 2, 3))
+    vol = np.einsum("ij,ij->i", a, np.cross(b, c)) / 6
+    assert np.all(vol > 0)
+    faces = {}
+    edges = set()
+    for tet in t:
+        for j in range(4):
+            f = tuple(sorted(tet[(j + k) % 4] for k in range(3)))
+            faces[f] = faces.get(f, 0) + 1
+        for i in range(4):
+            for k in range(i + 1, 4):
+                edges.add(tuple(sorted((tet[i], tet[k]))))
+    assert set(faces.values()) <= {1, 2}
+    bverts = {v for f, c in faces.items() if c == 1 for v in f}
+    assert np.allclose(np.linalg.norm(p[list(bverts)], axis=1), 1.0, atol=1e-14)
+    assert len(p) - len(edges) + len(faces) - len(t) == 1     # Euler characteristic of a ball
+
+
+def test_oracle_reproduces_the_ball_solution():
+    # u = (1 - |x|^2)/6 solves -Lap u = 1 (tests/unstructured/dg_tests.cpp:24-25
+    # with N = 3); P2 holds it exactly, so the error is the polyhedral boundary's
+    _lib_or_skip()
+    errs = []
+    for h in (0.5, 0.35, 0.25):
+        p, t = mgldg.ball_mesh(h)
+        pr = O.Problem.simplex(p, t, 3, 1 / h, 1 / h, agg_levels=1, seed=0)
+        A = R.to_scipy(pr.op(O.OP_A)).tocsc()
+        assert abs(A - A.T).max() <= 1e-13 * abs(A).max()
+        u = spla.spsolve(A, pr.rhs())
+        _, _, nodes = O.simplex_master(3, 3)
+        P0 = p[t[:, 0]]
+        J = np.stack([p[t[:, k]] - P0 for k in (1, 2, 3)], axis=2)
+        X = (P0[:, None, :] + np.einsum("eij,qj->eqi", J, nodes)).reshape(-1, 3)
+        errs.append(np.abs(u - (1 - (X ** 2).sum(1)) / 6).max())
+    assert errs[-1] < errs[0] / 2.5
