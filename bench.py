@@ -447,6 +447,105 @@ def run_unstructured(args, ctx, ext, torch, local, ws):
     return out
 
 
+def _field_at(X, seed, corr=0.2, sigma=0.5, nfeat=64):
+    """log-normal per-element diffusivity exp(g(x)), g a random-Fourier-feature
+    Gaussian field (correlation length corr, deviation sigma) -- the same
+    construction as the test's FP64 reference."""
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal((nfeat, X.shape[1])) / corr
+    ph = rng.uniform(0, 2 * np.pi, nfeat)
+    a = rng.standard_normal(nfeat) * sigma * np.sqrt(2.0 / nfeat)
+    return np.exp(np.cos(X @ w.T + ph) @ a)
+
+
+def run_adjoint(args, ctx, ext, torch, local, ws):
+    """P2 LDG on tetrahedra of the unit ball (ball mesher, h), per-element
+    diffusivity kappa_e = exp(g_e) (field seed 5011), u_obs the solution for a
+    perturbed kappa (seed 5012), loss 1/2 ||u - u_obs||^2: one step = forward
+    MG-PCG + adjoint MG-PCG on the same hierarchy + dL/dkappa, mixed precision,
+    RAT coarsening over the agglomeration hierarchy, Jacobi omega 0.7, V(2,2),
+    tol 1e-10."""
+    import mgldg
+    L = mgldg.lib()
+    h, P = args.ball_h, 3
+    dev = f"cuda:{local}"
+    t0 = time.perf_counter()
+    pts, tets = mgldg.ball_mesh(h)
+    prob = mgldg.CartesianProblem(ctx, P, mesh=(pts, tets), tau0=1 / h, tauD=1 / h, agg_levels=12, agg_seed=5000)
+    build_ms = (time.perf_counter() - t0) * 1e3
+    cent = pts[tets].mean(axis=1)
+    kappa = _field_at(cent, 5011)
+    k_true = _field_at(cent, 5012)
+    nlev = _coarse_levels(prob)
+    kw = dict(npre=2, npost=2, solver=mgldg.COARSE_DENSE, max_levels=nlev, mean_project=0,
+              relaxation=mgldg.RELAX_JACOBI, omega=0.7, restriction=mgldg.RESTRICT_RAT, precision=mgldg.PREC_MIXED)
+    n, ne = prob.ndof, prob.ne
+    b = torch.empty(n, dtype=torch.float64, device=dev)
+    u = torch.zeros_like(b)
+    lam = torch.zeros_like(b)
+    uobs = torch.zeros_like(b)
+    dk = torch.zeros(ne, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    ctx.check(L.mgldg_problem_rhs_gaussian_dev(ctx.h, prob.h, 5001, C.c_void_p(b.data_ptr())), "rhs")
+    ctx.sync()
+    it1 = C.c_int()
+    # observation: the solve with the perturbed diffusivity
+    prob.ops.construct_laplacian_kappa(k_true)
+    mg = mgldg.Multigrid(ctx, prob.ops, prob.T, **kw)
+    ctx.check(L.mgldg_pcg_dev(ctx.h, mg.h, prob.ops.A.h, C.c_void_p(b.data_ptr()), C.c_void_p(uobs.data_ptr()),
+                              1e-12, 400, C.byref(it1), np.zeros(400)), "pcg")
+    del mg
+    t0 = time.perf_counter()
+    prob.ops.construct_laplacian_kappa(kappa)
+    mg = mgldg.Multigrid(ctx, prob.ops, prob.T, **kw)
+    setup_ms = (time.perf_counter() - t0) * 1e3
+    loss = C.c_double()
+    its = (C.c_int * 2)()
+    p_ = lambda t: C.c_void_p(t.data_ptr())
+
+    def step():
+        with torch.cuda.stream(ext):
+            u.zero_()
+            lam.zero_()
+        ctx.check(L.mgldg_adjoint_l2_dev(ctx.h, mg.h, prob.ops.h, p_(b), p_(uobs), WL["tol"], 400, p_(u), p_(lam),
+                                         p_(dk), C.byref(loss), its), "adjoint")
+        return its[0], its[1]
+
+    for _ in range(max(1, args.warmup - 1)):
+        step()
+    ctx.sync()
+    dist_barrier(ws)
+    steps = max(1, min(args.steps, 3))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    for _ in range(steps):
+        itp = step()
+    e1.record(ext)
+    e1.synchronize()
+    ms = dist_max(e0.elapsed_time(e1) / steps, ws)
+    g = dk.cpu().numpy()
+    # check: true relative residual of the forward solution
+    r = torch.empty_like(b)
+    r.copy_(b)
+    torch.cuda.synchronize()
+    ctx.check(L.mgldg_bsr_mv_dev(ctx.h, -1.0, prob.ops.A.h, p_(u), 1.0, p_(r)), "mv")
+    ctx.sync()
+    rel_res = float(torch.linalg.norm(r) / torch.linalg.norm(b))
+    out = {
+        "workload": (f"unit ball, Kuhn cube grid mapped to the ball, h={h}: {ne:,} tetrahedra, P2 LDG (10 DOF/element, "
+                     f"{n:,} DOF), kappa_e = exp(g_e) (random-Fourier-feature field, corr 0.2, sigma 0.5, seed 5011), "
+                     f"u_obs from kappa seed 5012, L = 1/2 ||u - u_obs||^2; forward + adjoint MG-PCG on one hierarchy "
+                     f"({nlev} agglomeration levels, RAT, dense coarsest), mixed precision, Jacobi omega=0.7, V(2,2), "
+                     f"tol 1e-10, plus dL/dkappa"),
+        "ms_per_gradient": ms, "forward_iters": int(itp[0]), "adjoint_iters": int(itp[1]),
+        "loss": loss.value, "grad_norm": float(np.linalg.norm(g)), "forward_true_rel_residual": rel_res,
+        "problem_build_ms": build_ms, "operator_and_mg_setup_ms": setup_ms, "steps": steps,
+    }
+    del mg, prob, b, u, lam, uobs, dk, r
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_gpu(args, ws, rank, local):
     import torch
     import mgldg
@@ -623,6 +722,7 @@ def run_gpu(args, ws, rank, local):
     if args.batched > 0:
         batched = run_batched(args, ctx, ext, torch, local, ws)
     unstructured = run_unstructured(args, ctx, ext, torch, local, ws) if args.disk_batch > 0 else None
+    adjoint = run_adjoint(args, ctx, ext, torch, local, ws) if args.ball_h > 0 else None
 
     speedup = {}
     for sm in ("gs", "jacobi"):
@@ -654,6 +754,7 @@ def run_gpu(args, ws, rank, local):
         "roofline": roof,
         "batched": batched,
         "unstructured": unstructured,
+        "adjoint": adjoint,
         "gpu_launches": gpu_launches,
         "clocks": clk,
     }
@@ -675,6 +776,7 @@ def main():
     ap.add_argument("--batched-mesh", default="adaptive", choices=["adaptive", "uniform"])
     ap.add_argument("--disk-h", type=float, default=0.004, help="mesh size of the single unstructured disk")
     ap.add_argument("--disk-batch", type=int, default=48, help="meshes in the uneven batch (0: skip the line)")
+    ap.add_argument("--ball-h", type=float, default=0.03, help="tetrahedral ball mesh size of the adjoint line (0: skip)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
     args = ap.parse_args()
     ws, rank, local = dist_setup()

@@ -544,6 +544,59 @@ static void face_rule(int N, std::vector<double>& x, std::vector<double>& w) {
         }
 }
 
+// Cholesky factor of the aggregate's Gram matrix G = sum_u T_u^T M_u T_u
+// (row-major lower triangle; pivots below 1e-13 of the diagonal are raised to
+// that floor) and T_u <- T_u L^-T for its rows.  Plain double arithmetic in a
+// fixed order, the same as the oracle's.
+static void orthonormalize(const std::vector<int>& rows, std::vector<double>& vals, int br, int cb,
+                           const std::vector<SEl>* el, const std::vector<double>& Mref, double vref, double* Lout) {
+    std::vector<double> G((size_t)cb * cb, 0.0), MT((size_t)br * cb);
+    for (int u : rows) {
+        const double* T = &vals[(size_t)u * br * cb];
+        if (el) {
+            const double jac = (*el)[u].vol / vref;
+            for (int r = 0; r < br; ++r)
+                for (int c = 0; c < cb; ++c) {
+                    double s = 0;
+                    for (int k = 0; k < br; ++k) s += (Mref[(size_t)r * br + k] * jac) * T[(size_t)k * cb + c];
+                    MT[(size_t)r * cb + c] = s;
+                }
+        } else {
+            for (size_t k = 0; k < MT.size(); ++k) MT[k] = T[k];
+        }
+        for (int i = 0; i < cb; ++i)
+            for (int j = 0; j < cb; ++j) {
+                double s = 0;
+                for (int r = 0; r < br; ++r) s += T[(size_t)r * cb + i] * MT[(size_t)r * cb + j];
+                G[(size_t)i * cb + j] += s;
+            }
+    }
+    std::vector<double> L((size_t)cb * cb, 0.0);
+    for (int j = 0; j < cb; ++j) {
+        double d = G[(size_t)j * cb + j];
+        for (int k = 0; k < j; ++k) d -= L[(size_t)j * cb + k] * L[(size_t)j * cb + k];
+        const double floor = 1e-13 * G[(size_t)j * cb + j];
+        L[(size_t)j * cb + j] = std::sqrt(d > floor ? d : floor);
+        for (int i = j + 1; i < cb; ++i) {
+            double v = G[(size_t)i * cb + j];
+            for (int k = 0; k < j; ++k) v -= L[(size_t)i * cb + k] * L[(size_t)j * cb + k];
+            L[(size_t)i * cb + j] = v / L[(size_t)j * cb + j];
+        }
+    }
+    for (int u : rows) {
+        double* T = &vals[(size_t)u * br * cb];
+        for (int r = 0; r < br; ++r) {
+            double* t = T + (size_t)r * cb;
+            for (int j = 0; j < cb; ++j) {
+                double v = t[j];
+                for (int k = 0; k < j; ++k) v -= L[(size_t)j * cb + k] * t[k];
+                t[j] = v / L[(size_t)j * cb + j];
+            }
+        }
+    }
+    std::copy(L.begin(), L.end(), Lout);
+}
+
 mgldg_problem* simplex_problem(mgldg_ctx* ctx, int N, int np, const double* pts, int nt, const int* tris, int P,
                                double tau0, double tauD, int agg_levels, uint64_t agg_seed,
                                std::vector<std::vector<int>>* parts) {
@@ -917,6 +970,7 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int N, int np, const double* pts,
                     }
         };
         int nfine = nt;
+        std::vector<double> Lprev;   // per finer aggregate: its basis factor L
         for (int lev = 0; lev < agg_levels && nfine > 1; ++lev) {
             int nc = 0;
             std::vector<int> agg = greedy_agglomerate(nfine, adj, agg_seed + (uint64_t)lev, N, &nc);
@@ -980,6 +1034,33 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int N, int np, const double* pts,
                                 lagrangeN(x, E + (size_t)(row++) * cb);
                             }
                 }
+            }
+            // per aggregate, make the coarse basis orthonormal in the fine
+            // mass inner product: T_a <- T_a L_a^-T with L_a L_a^T =
+            // sum_{u in a} T_u^T M_u T_u (M_u the element mass on level 0;
+            // on coarser levels the previous coarse masses, the identity)
+            {
+                // rows first: the finer level's own basis change, T_u <- L_u^T T_u
+                if (lev > 0)
+                    for (int u = 0; u < nfine; ++u) {
+                        double* T = &vals[(size_t)u * br * cb];
+                        const double* Lu = &Lprev[(size_t)u * cb * cb];
+                        std::vector<double> tmp((size_t)br * cb);
+                        for (int r = 0; r < br; ++r)
+                            for (int c = 0; c < cb; ++c) {
+                                double sum = 0;
+                                for (int k = r; k < br; ++k) sum += Lu[(size_t)k * cb + r] * T[(size_t)k * cb + c];
+                                tmp[(size_t)r * cb + c] = sum;
+                            }
+                        std::copy(tmp.begin(), tmp.end(), T);
+                    }
+                std::vector<std::vector<int>> members(nc);
+                for (int u = 0; u < nfine; ++u) members[agg[u]].push_back(u);
+                std::vector<double> Lnext((size_t)nc * cb * cb);
+                for (int a = 0; a < nc; ++a)
+                    orthonormalize(members[a], vals, br, cb, lev == 0 ? &el : nullptr, MS.mass, MS.volume,
+                                   &Lnext[(size_t)a * cb * cb]);
+                Lprev.swap(Lnext);
             }
             pr->T.push_back(host_bsr(ctx, nfine, nc, br, cb, agg, vals));
             if (parts) parts->push_back(agg);

@@ -120,9 +120,14 @@ def test_agglomeration_covers_and_coarsens():
         n = len(counts)
     H = pr.hierarchy()
     assert (H[0].br, H[0].bc) == (6, 9) and all((T.br, T.bc) == (9, 9) for T in H[1:])
-    # interpolation of a constant is the constant
-    for T in H:
-        assert np.allclose(T.matvec(np.ones(T.nbc * T.bc)), 1.0, atol=1e-12)
+    # each aggregate's coarse basis is orthonormal in the fine mass inner
+    # product (T0^T M T0 = I), and the coarse space still holds the constants
+    M = R.to_scipy(pr.op(O.OP_M))
+    T0 = R.to_scipy(H[0])
+    G = (T0.T @ M @ T0).toarray()
+    assert np.abs(G - np.eye(len(G))).max() <= 1e-6
+    c, *_ = np.linalg.lstsq(T0.toarray(), np.ones(T0.shape[0]), rcond=None)
+    assert np.abs(T0 @ c - 1).max() <= 1e-8
 
 
 def test_ball_mesh_is_a_conforming_tetrahedralisation():

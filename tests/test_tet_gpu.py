@@ -5,7 +5,8 @@ transfers, right-hand sides, MG-PCG histories with RAT coarsening, the .fun
 dump, and the adjoint gradient dL/dkappa of a per-element diffusivity
 against the sparse-direct restatement and finite differences.
 
-Tolerances: operators 1e-13 of their largest entry; transfers 1e-14; rhs
+Tolerances: operators 1e-13 of their largest entry; transfers 1e-8 (see the
+test); rhs
 1e-14; PCG histories: the same iteration count, every ||r_k|| within
 1e-10 ||b|| (the coarse levels of bounding-box spaces reach cond ~ 1e6-1e7,
 so block inverses agree to cond * eps), solutions 1e-8; gradients 1e-7 of
@@ -53,8 +54,12 @@ def test_tet_hierarchy_rhs_and_dump_match_oracle(ctx, tmp_path):
         assert np.array_equal(prob.partition(l), pr.partition(l))
     H = pr.hierarchy()
     assert (H[0].br, H[0].bc) == (10, 27)
+    # the transfers' per-aggregate orthonormalisation goes through Cholesky
+    # factors of Gram matrices with cond up to ~1e8, whose inputs (the
+    # master mass matrices) differ between the two implementations in the
+    # last bit: agreement to cond * eps
     for Tg, Tr in zip(prob.T, H):
-        assert_same(Tg, Tr, 1e-14)
+        assert_same(Tg, Tr, 1e-8)
     b = prob.rhs_gaussian(5001)
     br = pr.rhs()
     assert np.abs(b - br).max() <= 1e-14 * np.abs(br).max()
