@@ -41,7 +41,7 @@ extern "C" {
 #define MGLDG_ERR_ARG         1  /* bad argument / unknown enum (multigrid.h:164,194,214) */
 #define MGLDG_ERR_SHAPE       2  /* block shapes do not conform (sparseblockmatrix.tpp:181-184) */
 #define MGLDG_ERR_CUDA        3  /* CUDA runtime failure */
-#define MGLDG_ERR_BREAKDOWN   4  /* PCG breakdown: d.q <= 0 or a non-finite scalar */
+#define MGLDG_ERR_BREAKDOWN   4  /* PCG breakdown: d.q <= 0, r.z < 0 or a non-finite scalar */
 #define MGLDG_ERR_TIMEOUT     5  /* a bounded device-side wait ran out */
 #define MGLDG_ERR_NOT_SPD     6  /* a block or the coarse matrix is singular / not SPD */
 #define MGLDG_ERR_NOMEM       7  /* device allocation failed */
@@ -78,6 +78,8 @@ int mgldg_bsr_create(mgldg_ctx* ctx, int nbr, int nbc, int br, int bc,
                      const int* row_ptr, const int* col_idx, const double* vals,
                      mgldg_bsr** A);
 int mgldg_bsr_destroy(mgldg_bsr* A);
+/* A device-side copy of A (pattern and values), owned by the caller. */
+int mgldg_bsr_clone(mgldg_ctx* ctx, const mgldg_bsr* A, mgldg_bsr** out);
 /* blockRows/blockCols/rowsPerBlock/colsPerBlock/nnzb (sparseblockmatrix.h:82-110) */
 int mgldg_bsr_info(const mgldg_bsr* A, int* nbr, int* nbc, int* br, int* bc,
                    int64_t* nnzb);

@@ -484,7 +484,7 @@ __global__ void k_bpcg_beta(int k, BatchScalars sc, const double* partials, int 
         sc.delta_old[c] = sc.delta_new[c];
         sc.delta_new[c] = rs;
         b = rs / sc.delta_old[c];
-        if (!isfinite(b)) {
+        if (!isfinite(b) || rs < 0.0) {   // r.z < 0: preconditioner not positive definite
             sc.broken[c] = 1;
             sc.active[c] = 0;
             b = 0;

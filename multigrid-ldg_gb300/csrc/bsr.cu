@@ -692,6 +692,15 @@ mgldg_bsr* bsr_clone(mgldg_ctx* ctx, const mgldg_bsr* A) {
 }  // namespace mg
 
 // ================================================================== C ABI ==
+extern "C" int mgldg_bsr_clone(mgldg_ctx* ctx, const mgldg_bsr* A, mgldg_bsr** out) {
+    MG_API_BEGIN(ctx)
+    MG_REQUIRE(A && out, MGLDG_ERR_ARG, "null argument");
+    *out = nullptr;
+    *out = bsr_clone(ctx, A);
+    sync(ctx);
+    MG_API_END
+}
+
 extern "C" int mgldg_bsr_create(mgldg_ctx* ctx, int nbr, int nbc, int br, int bc, const int* row_ptr,
                                 const int* col_idx, const double* vals, mgldg_bsr** out) {
     MG_API_BEGIN(ctx)

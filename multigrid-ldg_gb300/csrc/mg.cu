@@ -205,7 +205,7 @@ __global__ void k_pcg_init(PcgScalars* sc, const double* partials, int np) {
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sm[w];
         sc->delta_new = t;
         sc->delta0 = t;
-        sc->breakdown = 0;
+        sc->breakdown = t < 0.0 ? 1 : 0;   // r.z < 0: preconditioner not positive definite
     }
 }
 
@@ -250,7 +250,10 @@ __global__ void k_pcg_beta(PcgScalars* sc, const double* partials, int np) {
         sc->delta_old = sc->delta_new;
         sc->delta_new = rs;
         double b = rs / sc->delta_old;
-        if (!isfinite(b)) sc->breakdown = 1;
+        // r.z < 0: the preconditioner is not positive definite (for example
+        // a damped Jacobi smoother that diverges on some level); stop with an
+        // error instead of meeting the r.z test spuriously
+        if (!isfinite(b) || rs < 0.0) sc->breakdown = 1;
         sc->beta = b;
     }
 }
@@ -399,7 +402,8 @@ static void pcg_dev(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const doubl
     take_errors(m);
     const double tol2 = tol * tol;
     int i = 0;
-    bool broke = false;
+    bool broke = m->h_sc->breakdown != 0;
+    if (broke) maxit = 0;
     while (i < maxit && m->h_sc->delta_new > tol2 * m->h_sc->delta0) {
         // q = A d ; alpha = delta_new / d.q
         spmv<double>(ctx, A, 1.0, m->d, 0.0, nullptr, m->q, m->d, part, &np);
@@ -453,7 +457,7 @@ static void pcg_dev(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const doubl
         download(ctx, res_hist, m->hist, i);
         sync(ctx);
     }
-    if (broke) throw Error(MGLDG_ERR_BREAKDOWN, "pcg breakdown (d.q <= 0 or a non-finite scalar)");
+    if (broke) throw Error(MGLDG_ERR_BREAKDOWN, "pcg breakdown (d.q <= 0, r.z < 0 or a non-finite scalar)");
 }
 
 }  // namespace mg

@@ -43,7 +43,7 @@ EXPORTS = [
     "mgldg_quadtree_layer", "mgldg_h_points", "mgldg_seeded_points", "mgldg_quadtree_problem_create",
     "mgldg_problem_mesh_info", "mgldg_mesh_read", "mgldg_disk_mesh", "mgldg_simplex_problem_create",
     "mgldg_problem_partition", "mgldg_simplex_master", "mgldg_pcg_segmented_dev",
-    "mgldg_simplex_problem_create_nd", "mgldg_ball_mesh", "mgldg_simplex_master_nd",
+    "mgldg_simplex_problem_create_nd", "mgldg_ball_mesh", "mgldg_simplex_master_nd", "mgldg_bsr_clone",
 ]
 
 
@@ -101,6 +101,7 @@ def lib():
         L.mgldg_master_tables.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         L.mgldg_bsr_create.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, _ip, _ip, _dp, pvp]
         L.mgldg_bsr_destroy.argtypes = [vp]
+        L.mgldg_bsr_clone.argtypes = [vp, vp, pvp]
         L.mgldg_bsr_info.argtypes = [vp, ip, ip, ip, ip, i64p]
         L.mgldg_bsr_download.argtypes = [vp, vp, _ip, _ip, _dp]
         L.mgldg_bsr_mv.argtypes = [vp, C.c_double, vp, _dp, C.c_double, _dp]
@@ -256,6 +257,12 @@ class SparseBlockMatrix:
             v = np.zeros(1)
         ctx.check(lib().mgldg_bsr_create(ctx.h, nbr, nbc, br, bc, rp, ci, v, C.byref(h)), "bsr_create")
         return cls(ctx, h)
+
+    def clone(self):
+        """A device-side copy owned by the caller."""
+        h = C.c_void_p()
+        self.ctx.check(lib().mgldg_bsr_clone(self.ctx.h, self.h, C.byref(h)), "bsr_clone")
+        return SparseBlockMatrix(self.ctx, h)
 
     def info(self):
         a = [C.c_int() for _ in range(4)]
