@@ -46,7 +46,7 @@ def build(force=False, verbose=True):
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(_compile, srcs))
     tmp = LIB + ".tmp"
-    cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs
+    cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

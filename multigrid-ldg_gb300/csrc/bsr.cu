@@ -631,6 +631,18 @@ mgldg_bsr* bsr_transpose(mgldg_ctx* ctx, const mgldg_bsr* A) {
 void bsr_dedupe(mgldg_ctx* ctx, mgldg_bsr* A) {
     if (A->blk) return;
     const size_t bs = A->bsz();
+    // operators whose blocks are mostly distinct (transfers of unstructured
+    // hierarchies) are left as they are: look at a sample first
+    {
+        const int64_t ns = std::min<int64_t>(A->nnzb, 4096);
+        std::vector<double> hs((size_t)ns * bs);
+        download(ctx, hs.data(), A->val, hs.size());
+        sync(ctx);
+        std::unordered_map<std::string, int> sample;
+        for (int64_t k = 0; k < ns; ++k)
+            sample.emplace(std::string((const char*)(hs.data() + k * bs), bs * sizeof(double)), 0);
+        if (A->nnzb > 64 && (int64_t)sample.size() * 4 > ns) return;
+    }
     std::vector<double> h((size_t)A->nnzb * bs);
     download(ctx, h.data(), A->val, h.size());
     sync(ctx);

@@ -3,10 +3,15 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <cstring>
+#include <exception>
+#include <mutex>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/mgldg.h"
@@ -32,6 +37,52 @@ struct Error : std::runtime_error {
     do {                                            \
         if (!(cond)) throw ::mg::Error(code, msg);  \
     } while (0)
+
+// ------------------------------------------------------------ host threads --
+// parallel_ranges(n, grain, f): f(begin, end) over [0, n) in chunks of
+// `grain` on up to hardware_concurrency threads (the caller is one of them).
+// Every index is visited exactly once, so loops whose iterations write
+// disjoint outputs give the serial loop's result bit for bit.  The first
+// exception thrown by f is rethrown on the caller after all threads joined.
+template <class F>
+void parallel_ranges(int64_t n, int64_t grain, F&& f) {
+    if (n <= 0) return;
+    grain = std::max<int64_t>(1, grain);
+    const int64_t chunks = (n + grain - 1) / grain;
+    const int nth = (int)std::min<int64_t>(chunks, std::max(1u, std::min(std::thread::hardware_concurrency(), 64u)));
+    if (nth <= 1) {
+        f((int64_t)0, n);
+        return;
+    }
+    std::atomic<int64_t> next{0};
+    std::exception_ptr err;
+    std::mutex m;
+    auto work = [&]() {
+        try {
+            for (;;) {
+                const int64_t s = next.fetch_add(grain);
+                if (s >= n) break;
+                f(s, std::min(n, s + grain));
+            }
+        } catch (...) {
+            std::lock_guard<std::mutex> g(m);
+            if (!err) err = std::current_exception();
+            next.store(n);
+        }
+    };
+    std::vector<std::thread> th;
+    th.reserve(nth - 1);
+    for (int t = 1; t < nth; ++t) th.emplace_back(work);
+    work();
+    for (auto& t : th) t.join();
+    if (err) std::rethrow_exception(err);
+}
+template <class F>
+void parallel_for(int64_t n, int64_t grain, F&& f) {
+    parallel_ranges(n, grain, [&](int64_t s, int64_t e) {
+        for (int64_t i = s; i < e; ++i) f(i);
+    });
+}
 
 // --------------------------------------------------------------- profiling --
 struct ProfEvent {

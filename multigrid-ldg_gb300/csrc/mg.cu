@@ -11,7 +11,10 @@
 // the coarsest solve (mean projection and dense inverse), the outer CG
 // residuals, dot products and updates in FP64.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <mutex>
 #include <string>
 
@@ -553,6 +556,17 @@ extern "C" int mgldg_mg_create(mgldg_ctx* ctx, const mgldg_ops* fine, const mgld
     mgldg_mg* m = new mgldg_mg();
     m->ctx = ctx;
     m->p = p;
+    // MGLDG_SETUP_TRACE=1: phase times of the setup on stderr
+    static const bool trace = std::getenv("MGLDG_SETUP_TRACE") != nullptr;
+    auto t_last = std::chrono::steady_clock::now();
+    auto phase = [&](const char* what, int level) {
+        if (!trace) return;
+        sync(ctx);
+        const auto now = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "[mgldg setup] level %d %-12s %8.1f ms\n", level, what,
+                     std::chrono::duration<double, std::milli>(now - t_last).count());
+        t_last = now;
+    };
     try {
         const int use = (p.max_levels <= 0) ? nT : std::min(nT, p.max_levels - 1);
         m->L.resize(use + 1);
@@ -568,10 +582,13 @@ extern "C" int mgldg_mg_create(mgldg_ctx* ctx, const mgldg_ops* fine, const mgld
             mgldg_bsr* Tc = bsr_clone(ctx, Ti);
             m->L[i].T = Tc;
             bsr_dedupe(ctx, Tc);
+            phase("dedupe", i);
             m->L[i].Tt = bsr_transpose(ctx, Tc);
+            phase("transpose", i);
             mgldg_ops* c = (p.restriction == MGLDG_RESTRICT_RATRAT) ? galerkin_ratrat(ctx, f, Tc) : galerkin_rat(ctx, f, Tc);
             m->L[i + 1].ops = c;
             m->L[i + 1].owns_ops = true;
+            phase("galerkin", i);
             if (p.precision == MGLDG_PREC_MIXED) {
                 bsr_ensure_fp32(Tc);
                 bsr_ensure_fp32(m->L[i].Tt);
@@ -581,6 +598,7 @@ extern "C" int mgldg_mg_create(mgldg_ctx* ctx, const mgldg_ops* fine, const mgld
         for (int i = 0; i <= last; ++i) {
             bool sched = p.relaxation == MGLDG_RELAX_GAUSS_SEIDEL && (i < last || p.solver == MGLDG_COARSE_RELAXATION);
             level_alloc(ctx, m, m->L[i], sched);
+            phase("smoother", i);
         }
         if (p.solver != MGLDG_COARSE_RELAXATION) {
             const mgldg_bsr* Ac = m->L[last].A;
@@ -591,6 +609,7 @@ extern "C" int mgldg_mg_create(mgldg_ctx* ctx, const mgldg_ops* fine, const mgld
             MG_REQUIRE(m->nc <= 4096, MGLDG_ERR_UNSUPPORTED, "dense coarsest solve limited to 4096 unknowns");
             m->Cinv = dalloc<double>((size_t)m->nc * m->nc);
             dense_spd_inverse(ctx, Ac, m->Cinv);
+            phase("coarse", last);
         }
         sync(ctx);
     } catch (...) {

@@ -38,32 +38,68 @@ struct KeyTerm {
     Term t;
 };
 
-static void finish_plan(Plan& P, std::vector<KeyTerm>& kt, const std::vector<int64_t>* force_keys) {
-    // stable: keeps the generation order of terms inside one output block
-    std::stable_sort(kt.begin(), kt.end(), [](const KeyTerm& a, const KeyTerm& b) { return a.key < b.key; });
-    std::vector<int64_t> keys;
-    keys.reserve(kt.size() + (force_keys ? force_keys->size() : 0));
-    for (auto& e : kt) keys.push_back(e.key);
-    if (force_keys) keys.insert(keys.end(), force_keys->begin(), force_keys->end());
-    std::sort(keys.begin(), keys.end());
-    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
-    P.row_ptr.assign(P.nbr + 1, 0);
-    P.col_idx.resize(keys.size());
-    for (size_t q = 0; q < keys.size(); ++q) {
-        int i = (int)(keys[q] / P.nbc);
-        P.col_idx[q] = (int)(keys[q] - (int64_t)i * P.nbc);
-        P.row_ptr[i + 1]++;
+// Orders the terms by output block and builds the output pattern.  Terms go
+// to their output row by a stable counting sort, then each row is sorted
+// stably by key: the terms of one output block keep their generation order,
+// exactly as one global stable sort by key would leave them.
+static void finish_plan(Plan& P, std::vector<KeyTerm>& kt) {
+    const int nbr = P.nbr;
+    const int64_t nbc = P.nbc;
+    std::vector<int64_t> rp(nbr + 1, 0);
+    for (const KeyTerm& e : kt) rp[e.key / nbc + 1]++;
+    for (int i = 0; i < nbr; ++i) rp[i + 1] += rp[i];
+    std::vector<KeyTerm> s(kt.size());
+    {
+        std::vector<int64_t> pos(rp.begin(), rp.end() - 1);
+        for (const KeyTerm& e : kt) s[pos[e.key / nbc]++] = e;
     }
-    for (int i = 0; i < P.nbr; ++i) P.row_ptr[i + 1] += P.row_ptr[i];
-    P.tptr.assign(keys.size() + 1, 0);
-    P.terms.resize(kt.size());
-    size_t q = 0;
-    for (size_t e = 0; e < kt.size(); ++e) {
-        while (keys[q] != kt[e].key) ++q;
-        P.tptr[q + 1]++;
-        P.terms[e] = kt[e].t;
-    }
-    for (size_t o = 0; o < keys.size(); ++o) P.tptr[o + 1] += P.tptr[o];
+    std::vector<KeyTerm>().swap(kt);
+    std::vector<int> nk(nbr, 0);
+    parallel_for(nbr, 256, [&](int64_t i) {
+        auto b = s.begin() + rp[i], e = s.begin() + rp[i + 1];
+        std::stable_sort(b, e, [](const KeyTerm& x, const KeyTerm& y) { return x.key < y.key; });
+        int c = 0;
+        for (auto it = b; it != e; ++it)
+            if (it == b || it->key != (it - 1)->key) ++c;
+        nk[i] = c;
+    });
+    P.row_ptr.assign(nbr + 1, 0);
+    for (int i = 0; i < nbr; ++i) P.row_ptr[i + 1] = P.row_ptr[i] + nk[i];
+    const int nkeys = P.row_ptr[nbr];
+    P.col_idx.resize(nkeys);
+    P.tptr.assign((size_t)nkeys + 1, 0);
+    P.terms.resize(s.size());
+    parallel_for(nbr, 256, [&](int64_t i) {
+        int q = P.row_ptr[i] - 1;
+        for (int64_t t = rp[i]; t < rp[i + 1]; ++t) {
+            if (t == rp[i] || s[t].key != s[t - 1].key) {
+                ++q;
+                P.col_idx[q] = (int)(s[t].key - i * nbc);
+            }
+            P.tptr[q + 1]++;
+            P.terms[t] = s[t].t;
+        }
+    });
+    for (int o = 0; o < nkeys; ++o) P.tptr[o + 1] += P.tptr[o];
+}
+
+// Re-indexes P's terms onto the pattern of U (which holds P's pattern):
+// output blocks of U that P lacks get no terms.
+static void expand_plan(Plan& P, const Plan& U) {
+    std::vector<int> cnt((size_t)U.row_ptr[U.nbr], 0);
+    parallel_for(U.nbr, 256, [&](int64_t i) {
+        int p = P.row_ptr[i];
+        for (int q = U.row_ptr[i]; q < U.row_ptr[i + 1]; ++q)
+            if (p < P.row_ptr[i + 1] && P.col_idx[p] == U.col_idx[q]) {
+                cnt[q] = P.tptr[p + 1] - P.tptr[p];
+                ++p;
+            }
+        MG_REQUIRE(p == P.row_ptr[i + 1], MGLDG_ERR_SHAPE, "product pattern is not contained in the union");
+    });
+    P.row_ptr = U.row_ptr;
+    P.col_idx = U.col_idx;
+    P.tptr.assign(cnt.size() + 1, 0);
+    for (size_t q = 0; q < cnt.size(); ++q) P.tptr[q + 1] = P.tptr[q] + cnt[q];
 }
 
 // C = op(X) * Y   (multiply_mm when !tX, multiply_mm_t when tX)
@@ -100,7 +136,7 @@ static Plan plan_mm(const mgldg_bsr* X, bool tX, const mgldg_bsr* Y) {
                     kt.push_back({(int64_t)i * P.nbc + Y->h_col_idx[b], Term{a, -1, b}});
             }
     }
-    finish_plan(P, kt, nullptr);
+    finish_plan(P, kt);
     return P;
 }
 
@@ -111,39 +147,43 @@ static Plan plan_triple(const std::vector<const mgldg_bsr*>& Xs, const mgldg_bsr
                         std::vector<Plan>* per_dim) {
     const mgldg_bsr* X0 = Xs[0];
     int nout = X0->nbc;
-    std::vector<int64_t> allkeys;
-    std::vector<std::vector<KeyTerm>> kts(Xs.size());
+    per_dim->clear();
     for (size_t d = 0; d < Xs.size(); ++d) {
         const mgldg_bsr* X = Xs[d];
         MG_REQUIRE(X->nbr == D->nbr && X->br == D->bc, MGLDG_ERR_SHAPE, "triple product: shapes do not conform");
+        std::vector<KeyTerm> kt;
         for (int k = 0; k < X->nbr; ++k) {
             int m = D->h_diag[k];
             MG_REQUIRE(m >= 0, MGLDG_ERR_SHAPE, "mass matrix lacks a diagonal block");
             for (int a = X->h_row_ptr[k]; a < X->h_row_ptr[k + 1]; ++a)
-                for (int b = X->h_row_ptr[k]; b < X->h_row_ptr[k + 1]; ++b) {
-                    int64_t key = (int64_t)X->h_col_idx[a] * nout + X->h_col_idx[b];
-                    kts[d].push_back({key, Term{a, m, b}});
-                    allkeys.push_back(key);
-                }
+                for (int b = X->h_row_ptr[k]; b < X->h_row_ptr[k + 1]; ++b)
+                    kt.push_back({(int64_t)X->h_col_idx[a] * nout + X->h_col_idx[b], Term{a, m, b}});
         }
-    }
-    if (extra)
-        for (int i = 0; i < extra->nbr; ++i)
-            for (int a = extra->h_row_ptr[i]; a < extra->h_row_ptr[i + 1]; ++a)
-                allkeys.push_back((int64_t)i * nout + extra->h_col_idx[a]);
-    std::sort(allkeys.begin(), allkeys.end());
-    allkeys.erase(std::unique(allkeys.begin(), allkeys.end()), allkeys.end());
-    Plan U;
-    U.nbr = nout; U.nbc = nout;
-    std::vector<KeyTerm> none;
-    finish_plan(U, none, &allkeys);
-    per_dim->clear();
-    for (size_t d = 0; d < Xs.size(); ++d) {
         Plan P;
         P.nbr = nout; P.nbc = nout;
-        finish_plan(P, kts[d], &allkeys);
+        finish_plan(P, kt);
         per_dim->push_back(std::move(P));
     }
+    // the union pattern: every dimension's blocks and `extra`'s (the T pattern)
+    Plan U;
+    U.nbr = nout; U.nbc = nout;
+    std::vector<std::vector<int>> cols(nout);
+    parallel_for(nout, 256, [&](int64_t i) {
+        std::vector<int>& c = cols[i];
+        for (const Plan& P : *per_dim) c.insert(c.end(), P.col_idx.begin() + P.row_ptr[i], P.col_idx.begin() + P.row_ptr[i + 1]);
+        if (extra && i < extra->nbr)
+            c.insert(c.end(), extra->h_col_idx.begin() + extra->h_row_ptr[i], extra->h_col_idx.begin() + extra->h_row_ptr[i + 1]);
+        std::sort(c.begin(), c.end());
+        c.erase(std::unique(c.begin(), c.end()), c.end());
+    });
+    U.row_ptr.assign(nout + 1, 0);
+    for (int i = 0; i < nout; ++i) U.row_ptr[i + 1] = U.row_ptr[i] + (int)cols[i].size();
+    U.col_idx.resize(U.row_ptr[nout]);
+    parallel_for(nout, 256, [&](int64_t i) {
+        std::copy(cols[i].begin(), cols[i].end(), U.col_idx.begin() + U.row_ptr[i]);
+    });
+    U.tptr.assign((size_t)U.row_ptr[nout] + 1, 0);
+    for (Plan& P : *per_dim) expand_plan(P, U);
     return U;
 }
 
@@ -599,6 +639,67 @@ __global__ void __launch_bounds__(1024) k_gauss_jordan(int n, double* aug, int* 
         __syncthreads();
     }
 }
+// The same elimination for larger n, one pivot column per pair of launches:
+// k_gj_pivot (one CTA) picks the pivot row, swaps it into row k, saves the
+// column-k factors f[r] and scales row k; k_gj_eliminate (all SMs) subtracts
+// f[r] times row k from every other row and zeroes column k.
+__global__ void __launch_bounds__(1024) k_gj_pivot(int n, int k, double* aug, double* f, int* status) {
+    __shared__ double sv[32];
+    __shared__ int si[32];
+    __shared__ int piv;
+    __shared__ double pinv;
+    const int w2 = 2 * n;
+    double v = -1.0;
+    int idx = n;
+    for (int r = k + threadIdx.x; r < n; r += blockDim.x) {
+        const double a = fabs(aug[(size_t)r * w2 + k]);
+        if (a > v) { v = a; idx = r; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double v2 = __shfl_xor_sync(0xffffffffu, v, o);
+        const int i2 = __shfl_xor_sync(0xffffffffu, idx, o);
+        if (v2 > v || (v2 == v && i2 < idx)) { v = v2; idx = i2; }
+    }
+    if ((threadIdx.x & 31) == 0) { sv[threadIdx.x >> 5] = v; si[threadIdx.x >> 5] = idx; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double bv = -1.0;
+        int bi = n;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+            if (sv[w] > bv || (sv[w] == bv && si[w] < bi)) { bv = sv[w]; bi = si[w]; }
+        if (!(bv > 0.0) || !isfinite(bv) || bi >= n) { *status = 1; bi = k; }
+        piv = bi;
+    }
+    __syncthreads();
+    const int p = piv;
+    if (p != k)
+        for (int c = threadIdx.x; c < w2; c += blockDim.x) {
+            const double t = aug[(size_t)k * w2 + c];
+            aug[(size_t)k * w2 + c] = aug[(size_t)p * w2 + c];
+            aug[(size_t)p * w2 + c] = t;
+        }
+    __syncthreads();
+    for (int r = threadIdx.x; r < n; r += blockDim.x) f[r] = (r == k) ? 0.0 : aug[(size_t)r * w2 + k];
+    if (threadIdx.x == 0) pinv = 1.0 / aug[(size_t)k * w2 + k];
+    __syncthreads();
+    for (int c = threadIdx.x; c < w2; c += blockDim.x) aug[(size_t)k * w2 + c] *= pinv;
+}
+
+__global__ void __launch_bounds__(256) k_gj_eliminate(int n, int k, double* __restrict__ aug,
+                                                     const double* __restrict__ f) {
+    const int w2 = 2 * n;
+    const double* __restrict__ pk = aug + (size_t)k * w2;
+    for (int r = blockIdx.y; r < n; r += gridDim.y) {
+        if (r == k) continue;
+        const double fr = f[r];
+        if (fr == 0.0) continue;
+        double* row = aug + (size_t)r * w2;
+        for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < w2; c += gridDim.x * blockDim.x)
+            row[c] = (c == k) ? 0.0 : row[c] - fr * pk[c];
+    }
+}
+
 __global__ void k_extract_right(int n, const double* aug, double* out) {
     for (int r = blockIdx.x; r < n; r += gridDim.x)
         for (int c = threadIdx.x; c < n; c += blockDim.x) out[(size_t)r * n + c] = aug[(size_t)r * 2 * n + n + c];
@@ -624,9 +725,27 @@ void dense_spd_inverse(mgldg_ctx* ctx, const mgldg_bsr* A, double* out_inv) {
             Launch L(ctx, MGLDG_K_SETUP);
             k_identity_right<<<std::min(n, 1024), 256, 0, ctx->stream>>>(n, aug);
         }
-        {
+        if (n <= 128) {
             Launch L(ctx, MGLDG_K_SETUP);
             k_gauss_jordan<<<1, 1024, 0, ctx->stream>>>(n, aug, dstatus);
+        } else {
+            double* f = dalloc<double>(n);
+            try {
+                const dim3 grid((unsigned)std::min(8, (2 * n + 255) / 256), (unsigned)std::min(n, ctx->sm_count * 8));
+                Launch L(ctx, MGLDG_K_SETUP);
+                for (int k = 0; k < n; ++k) {
+                    k_gj_pivot<<<1, 1024, 0, ctx->stream>>>(n, k, aug, f, dstatus);
+                    k_gj_eliminate<<<grid, 256, 0, ctx->stream>>>(n, k, aug, f);
+                }
+                check_launch();
+                ctx->launches[MGLDG_K_SETUP] += 2 * (int64_t)n - 1;
+                ctx->lv_launches[MGLDG_K_SETUP][L.lv] += 2 * (int64_t)n - 1;
+            } catch (...) {
+                dfree(f);
+                throw;
+            }
+            sync(ctx);
+            dfree(f);
         }
         {
             Launch L(ctx, MGLDG_K_SETUP);

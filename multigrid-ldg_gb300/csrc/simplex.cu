@@ -22,8 +22,10 @@
 // are homogeneous Dirichlet.
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <fstream>
 #include <map>
 #include <random>
@@ -83,6 +85,7 @@ struct SMaster {
     std::vector<std::array<int, 3>> idx;     // node multi-indices
     std::vector<std::array<int, 3>> mono;    // monomial exponents
     std::vector<LD> C;                       // b x b, C[m*b + i]
+    std::vector<double> Cd;                  // C rounded to double (for eval)
     std::vector<double> nodes;               // b x N
     std::vector<double> mass, invmass, diff[3];
     SMaster(int N_, int P_) : N(N_), P(P_) {
@@ -111,6 +114,7 @@ struct SMaster {
         for (int q = 0; q < b; ++q)
             for (int m = 0; m < b; ++m) C[(size_t)q * b + m] = mono_val(m, &xn[(size_t)q * 3]);
         ld_inverse(C, b);
+        Cd.assign(C.begin(), C.end());
         // mass: exact monomial integrals over the master simplex
         // (a! b! c! / (a + b + c + N)!)
         auto integral = [&](int a0, int a1, int a2) -> LD {
@@ -161,14 +165,20 @@ struct SMaster {
                 for (int k = 0; k < mono[m][o]; ++k) v *= x[o];
         return v;
     }
-    // nodal basis at x (N doubles in)
+    // nodal basis at x (N doubles in), in double: the monomials at x once,
+    // then phi_i = sum_m C(m,i) x^m (b <= 56, exponents <= 5)
     void eval(const double* x, double* out) const {
-        LD xl[3] = {0, 0, 0};
-        for (int d = 0; d < N; ++d) xl[d] = x[d];
+        double pw[3][8];
+        for (int d = 0; d < 3; ++d) {
+            pw[d][0] = 1.0;
+            for (int k = 1; k < 8; ++k) pw[d][k] = pw[d][k - 1] * (d < N ? x[d] : 0.0);
+        }
+        double mv[64];
+        for (int m = 0; m < b; ++m) mv[m] = pw[0][mono[m][0]] * pw[1][mono[m][1]] * pw[2][mono[m][2]];
         for (int i = 0; i < b; ++i) {
-            LD sum = 0;
-            for (int m = 0; m < b; ++m) sum += C[(size_t)m * b + i] * mono_val(m, xl);
-            out[i] = (double)sum;
+            double sum = 0;
+            for (int m = 0; m < b; ++m) sum += Cd[(size_t)m * b + i] * mv[m];
+            out[i] = sum;
         }
     }
     int index_of(int i0, int i1, int i2 = 0) const {
@@ -607,6 +617,16 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int N, int np, const double* pts,
     const int nv = N + 1;
     for (int64_t k = 0; k < (int64_t)nv * nt; ++k)
         MG_REQUIRE(tris[k] >= 0 && tris[k] < np, MGLDG_ERR_ARG, "vertex index out of range");
+    static const bool trace = std::getenv("MGLDG_SETUP_TRACE") != nullptr;
+    auto t_last = std::chrono::steady_clock::now();
+    auto phase = [&](const char* what) {
+        if (!trace) return;
+        sync(ctx);
+        const auto now = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "[mgldg build] %-14s %8.1f ms\n", what,
+                     std::chrono::duration<double, std::milli>(now - t_last).count());
+        t_last = now;
+    };
     const SMaster MS(N, P), MF(N - 1, P);
     const int b = MS.b, P1 = MF.b;
     std::vector<SEl> el(nt);
@@ -717,6 +737,7 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int N, int np, const double* pts,
     }
     const int nf = (int)faces.size();
     const int nfi = nf - nb;
+    phase("faces");
 
     // ---- contributions: elements (M, G_d), interior faces (2N + 4),
     // boundary faces (N + 1)
@@ -736,9 +757,9 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int N, int np, const double* pts,
     face_rule(N, qx, qw);
     const int nq = (int)qw.size();
     std::vector<double> bvals((size_t)nkb * nb * bsz);
-    {
+    parallel_ranges(nb, 64, [&](int64_t q0, int64_t q1) {
         std::vector<double> phl((size_t)nq * b), Lm((size_t)b * nq), LL(bsz), Minv(bsz);
-        for (int q = 0; q < nb; ++q) {
+        for (int64_t q = q0; q < q1; ++q) {
             const HF& f = faces[boundary[q]];
             const SEl& s = el[f.left];
             for (int k = 0; k < nq; ++k) {
@@ -780,8 +801,9 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int N, int np, const double* pts,
             double* T = &bvals[((size_t)nkb * q + N) * bsz];
             for (size_t k = 0; k < bsz; ++k) T[k] = tauD * LL[k];
         }
-    }
+    });
 
+    phase("boundary");
     // per stored block, its contributions in the reference's order
     struct Tr {
         int row, col;
@@ -831,11 +853,15 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int N, int np, const double* pts,
         }
         return As;
     };
-    const Assembly AM = assemble(tm);
-    std::vector<Assembly> AG;
-    for (int d = 0; d < N; ++d) AG.push_back(assemble(tg[d]));
-    const Assembly AT = assemble(tt);
+    Assembly AM, AT;
+    std::vector<Assembly> AG(N);
+    parallel_for(N + 2, 1, [&](int64_t w) {
+        if (w == 0) AM = assemble(tm);
+        else if (w <= N) AG[w - 1] = assemble(tg[w - 1]);
+        else AT = assemble(tt);
+    });
 
+    phase("lists");
     // ---- GPU: contributions, then the operators ----
     mgldg_problem* pr = new mgldg_problem();
     pr->ctx = ctx;
@@ -911,6 +937,7 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int N, int np, const double* pts,
                                                        d_contrib + (size_t)c_face * bsz);
         }
         check_launch();
+        phase("gpu blocks");
         M = realize(ctx, AM, nt, b, d_contrib);
         for (int d = 0; d < N; ++d) Gs.push_back(realize(ctx, AG[d], nt, b, d_contrib));
         Tm = realize(ctx, AT, nt, b, d_contrib);
@@ -923,7 +950,9 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int N, int np, const double* pts,
             Gs[d] = nullptr;
         }
         pr->ops->T = Tm; Tm = nullptr;
+        phase("realize");
         construct_laplacian(ctx, pr->ops);
+        phase("laplacian");
         // geometry for right-hand sides and dumps
         pr->sgeom = geom;
         pr->snodes = MS.nodes;
@@ -975,6 +1004,7 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int N, int np, const double* pts,
             int nc = 0;
             std::vector<int> agg = greedy_agglomerate(nfine, adj, agg_seed + (uint64_t)lev, N, &nc);
             if (nc >= nfine) break;
+            phase("  agglomerate");
             const std::vector<SBox>& src = lev == 0 ? box : fbox;
             std::vector<SBox> cbox(nc);
             std::vector<char> seen(nc, 0);
@@ -994,7 +1024,7 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int N, int np, const double* pts,
             }
             const int br = lev == 0 ? b : cb;
             std::vector<double> vals((size_t)nfine * br * cb, 0.0);
-            for (int u = 0; u < nfine; ++u) {
+            parallel_for(nfine, 1024, [&](int64_t u) {
                 const int a = agg[u];
                 const SBox& B = cbox[a];
                 double w[3];
@@ -1034,7 +1064,7 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int N, int np, const double* pts,
                                 lagrangeN(x, E + (size_t)(row++) * cb);
                             }
                 }
-            }
+            });
             // per aggregate, make the coarse basis orthonormal in the fine
             // mass inner product: T_a <- T_a L_a^-T with L_a L_a^T =
             // sum_{u in a} T_u^T M_u T_u (M_u the element mass on level 0;
@@ -1042,27 +1072,33 @@ mgldg_problem* simplex_problem(mgldg_ctx* ctx, int N, int np, const double* pts,
             {
                 // rows first: the finer level's own basis change, T_u <- L_u^T T_u
                 if (lev > 0)
-                    for (int u = 0; u < nfine; ++u) {
-                        double* T = &vals[(size_t)u * br * cb];
-                        const double* Lu = &Lprev[(size_t)u * cb * cb];
+                    parallel_ranges(nfine, 256, [&](int64_t u0, int64_t u1) {
                         std::vector<double> tmp((size_t)br * cb);
-                        for (int r = 0; r < br; ++r)
-                            for (int c = 0; c < cb; ++c) {
-                                double sum = 0;
-                                for (int k = r; k < br; ++k) sum += Lu[(size_t)k * cb + r] * T[(size_t)k * cb + c];
-                                tmp[(size_t)r * cb + c] = sum;
-                            }
-                        std::copy(tmp.begin(), tmp.end(), T);
-                    }
+                        for (int64_t u = u0; u < u1; ++u) {
+                            double* T = &vals[(size_t)u * br * cb];
+                            const double* Lu = &Lprev[(size_t)u * cb * cb];
+                            for (int r = 0; r < br; ++r)
+                                for (int c = 0; c < cb; ++c) {
+                                    double sum = 0;
+                                    for (int k = r; k < br; ++k) sum += Lu[(size_t)k * cb + r] * T[(size_t)k * cb + c];
+                                    tmp[(size_t)r * cb + c] = sum;
+                                }
+                            std::copy(tmp.begin(), tmp.end(), T);
+                        }
+                    });
+                phase("  basis");
                 std::vector<std::vector<int>> members(nc);
                 for (int u = 0; u < nfine; ++u) members[agg[u]].push_back(u);
                 std::vector<double> Lnext((size_t)nc * cb * cb);
-                for (int a = 0; a < nc; ++a)
+                parallel_for(nc, 64, [&](int64_t a) {
                     orthonormalize(members[a], vals, br, cb, lev == 0 ? &el : nullptr, MS.mass, MS.volume,
                                    &Lnext[(size_t)a * cb * cb]);
+                });
                 Lprev.swap(Lnext);
             }
+            phase("  orthonormal");
             pr->T.push_back(host_bsr(ctx, nfine, nc, br, cb, agg, vals));
+            phase("  upload");
             if (parts) parts->push_back(agg);
             adj = coarse_graph(adj, agg, nc);
             fbox = cbox;
