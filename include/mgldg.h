@@ -262,10 +262,16 @@ int mgldg_problem_mesh_info(const mgldg_problem* pr, int* nfaces, int* nbfaces, 
  * x y, an empty line, nt lines of 1-based vertex triples; p[2*np], t[3*nt]
  * 0-based (pass p = t = NULL to get the counts first).  mgldg_disk_mesh (no
  * reference counterpart; the reference reads distmesh output) meshes the
- * unit disk with concentric rings of spacing 1/ceil(1/h), same calling
- * pattern. */
+ * unit disk with concentric rings of spacing 1/ceil(1/h), triangles in the
+ * Morton order below, same calling pattern. */
 int mgldg_mesh_read(const char* path, int* np, int* nt, double* p, int* t);
 int mgldg_disk_mesh(double h, int* np, int* nt, double* p, int* t);
+/* Reorders the N-simplices t[(N+1)*nt] in place, stably, by the Morton key
+ * of their centroids (no reference counterpart).  Element order is block
+ * Gauss-Seidel's order: an order whose dependency chain is as long as the
+ * mesh (a ring around a disk, with the LDG operator's two-element reach)
+ * serialises the sweep; a space-filling order keeps the chain short. */
+int mgldg_mesh_morton_order(int N, int np, const double* p, int nt, int* t);
 /* P_{P-1} LDG on a triangle mesh (Mesh(wireframe), mesh.h:187-300;
  * LDGPoisson::discretize, ldgpoisson.tpp:27-100), homogeneous Dirichlet on
  * every boundary edge, P in 1..4 (b = P(P+1)/2 unknowns per element), with

@@ -1139,6 +1139,46 @@ void simplex_rhs_dev(mgldg_ctx* ctx, const mgldg_problem* pr, uint64_t seed, dou
 // max(6k, round(2 pi k)) equally spaced points starting at angle 0, and the
 // strip between rings k-1 and k triangulated by advancing whichever ring's
 // next point has the smaller angle.  Counter-clockwise triangles.
+// Elements sorted (stably) by the Morton key of their centroid: 2^(63/N)
+// cells per axis over the centroids' bounding box, bits interleaved with x
+// highest.  The element order is the order of block Gauss-Seidel, whose
+// sweep is a chain of dependencies through neighbours that come earlier;
+// orders that close a loop (a ring around the disk) make that chain as long
+// as the mesh, a space-filling order keeps it near the mesh's diameter.
+static void morton_order(int N, const double* p, int nt, int* t) {
+    const int nv = N + 1, bits = 63 / N;
+    std::vector<double> c((size_t)nt * N, 0.0);
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int e = 0; e < nt; ++e)
+        for (int d = 0; d < N; ++d) {
+            double s = 0;
+            for (int v = 0; v < nv; ++v) s += p[(size_t)N * t[(size_t)nv * e + v] + d];
+            s /= nv;
+            c[(size_t)N * e + d] = s;
+            lo[d] = std::min(lo[d], s);
+            hi[d] = std::max(hi[d], s);
+        }
+    const double cells = std::ldexp(1.0, bits);
+    std::vector<std::pair<uint64_t, int>> key(nt);
+    for (int e = 0; e < nt; ++e) {
+        uint64_t q[3] = {0, 0, 0};
+        for (int d = 0; d < N; ++d) {
+            const double w = hi[d] - lo[d];
+            const double f = w > 0 ? (c[(size_t)N * e + d] - lo[d]) / w : 0.0;
+            q[d] = (uint64_t)std::min(cells - 1, std::max(0.0, std::floor(f * cells)));
+        }
+        uint64_t k = 0;
+        for (int b = bits - 1; b >= 0; --b)
+            for (int d = 0; d < N; ++d) k = (k << 1) | ((q[d] >> b) & 1u);
+        key[e] = {k, e};
+    }
+    std::stable_sort(key.begin(), key.end(),
+                     [](const std::pair<uint64_t, int>& a, const std::pair<uint64_t, int>& b) { return a.first < b.first; });
+    std::vector<int> old(t, t + (size_t)nv * nt);
+    for (int e = 0; e < nt; ++e)
+        for (int v = 0; v < nv; ++v) t[(size_t)nv * e + v] = old[(size_t)nv * key[e].second + v];
+}
+
 static void disk_mesh(double h, std::vector<double>& p, std::vector<int>& t) {
     MG_REQUIRE(h > 0 && h <= 1, MGLDG_ERR_ARG, "mesh size must be in (0, 1]");
     const int K = (int)std::ceil(1.0 / h - 1e-12);
@@ -1187,12 +1227,14 @@ static void disk_mesh(double h, std::vector<double>& p, std::vector<int>& t) {
             }
         }
     }
+    morton_order(2, p.data(), (int)t.size() / 3, t.data());
 }
 
 // Ball mesher (no reference counterpart): the cube [-1,1]^3 on an n^3 grid
 // (n = ceil(1.4/h)), every cube cut into the six tetrahedra of its Kuhn
 // triangulation (conforming across cubes), vertices mapped onto the ball by
-// x -> x |x|_inf / |x|_2.  Positively oriented tetrahedra.
+// x -> x |x|_inf / |x|_2.  Positively oriented tetrahedra, cube by cube in
+// lexicographic order.
 static void ball_mesh(double h, std::vector<double>& p, std::vector<int>& t) {
     MG_REQUIRE(h > 0 && h <= 2, MGLDG_ERR_ARG, "mesh size must be in (0, 2]");
     const int n = std::max(1, (int)std::ceil(1.4 / h - 1e-12));
@@ -1359,6 +1401,18 @@ extern "C" int mgldg_simplex_master(int N, int P, double* mass, double* diff0, d
         std::copy(m.nodes.begin(), m.nodes.end(), nodes);
     } catch (const Error& e) {
         return e.code;
+    }
+    return MGLDG_OK;
+}
+
+extern "C" int mgldg_mesh_morton_order(int N, int np, const double* p, int nt, int* t) {
+    if ((N != 2 && N != 3) || np < 1 || nt < 0 || !p || (nt > 0 && !t)) return MGLDG_ERR_ARG;
+    for (int64_t k = 0; k < (int64_t)(N + 1) * nt; ++k)
+        if (t[k] < 0 || t[k] >= np) return MGLDG_ERR_ARG;
+    try {
+        morton_order(N, p, nt, t);
+    } catch (const std::bad_alloc&) {
+        return MGLDG_ERR_NOMEM;
     }
     return MGLDG_OK;
 }

@@ -41,7 +41,7 @@ EXPORTS = [
     "mgldg_bsr_mm_dev", "mgldg_mg_vcycle_batched_dev", "mgldg_pcg_batched_dev", "mgldg_pcg_batched",
     "mgldg_mg_batch_tiles", "mgldg_quadtree_create", "mgldg_quadtree_destroy", "mgldg_quadtree_info",
     "mgldg_quadtree_layer", "mgldg_h_points", "mgldg_seeded_points", "mgldg_quadtree_problem_create",
-    "mgldg_problem_mesh_info", "mgldg_mesh_read", "mgldg_disk_mesh", "mgldg_simplex_problem_create",
+    "mgldg_problem_mesh_info", "mgldg_mesh_read", "mgldg_disk_mesh", "mgldg_mesh_morton_order", "mgldg_simplex_problem_create",
     "mgldg_problem_partition", "mgldg_simplex_master", "mgldg_pcg_segmented_dev",
     "mgldg_simplex_problem_create_nd", "mgldg_ball_mesh", "mgldg_simplex_master_nd", "mgldg_bsr_clone",
 ]
@@ -169,6 +169,7 @@ def lib():
         L.mgldg_simplex_problem_create_nd.argtypes = [vp, C.c_int, C.c_int, _dp, C.c_int, _ip, C.c_int, C.c_double,
                                                       C.c_double, C.c_int, C.c_uint64, pvp]
         L.mgldg_ball_mesh.argtypes = [C.c_double, ip, ip, vp, vp]
+        L.mgldg_mesh_morton_order.argtypes = [C.c_int, C.c_int, vp, C.c_int, vp]
         L.mgldg_simplex_master_nd.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp]
         L.mgldg_pcg_segmented_dev.argtypes = [vp, vp, vp, C.c_int, C.POINTER(C.c_int64), vp, vp, C.c_double,
                                               C.c_int, _ip, _dp]
@@ -593,6 +594,18 @@ def _two_call(fn, *head, N=2):
 def disk_mesh(h):
     """Triangles of the unit disk with spacing about h: (points[np,2], triangles[nt,3])."""
     return _two_call(lib().mgldg_disk_mesh, C.c_double(h))
+
+
+def morton_order(p, t):
+    """Elements of (p, t) reordered stably by the Morton key of their
+    centroids (the block Gauss-Seidel order; see mgldg_mesh_morton_order)."""
+    p = np.ascontiguousarray(p, np.float64)
+    t = np.array(t, dtype=np.int32, order="C")
+    N = p.shape[1]
+    rc = lib().mgldg_mesh_morton_order(N, len(p), p.ctypes.data_as(C.c_void_p), len(t), t.ctypes.data_as(C.c_void_p))
+    if rc:
+        raise MgldgError(rc, "mesh_morton_order")
+    return t
 
 
 def ball_mesh(h):

@@ -168,3 +168,31 @@ def test_oracle_reproduces_the_ball_solution():
         X = (P0[:, None, :] + np.einsum("eij,qj->eqi", J, nodes)).reshape(-1, 3)
         errs.append(np.abs(u - (1 - (X ** 2).sum(1)) / 6).max())
     assert errs[-1] < errs[0] / 2.5
+
+
+def test_morton_order_is_a_stable_permutation_and_keeps_gauss_seidel_chains_short():
+    _lib_or_skip()
+    p, t = mgldg.disk_mesh(0.05)
+    # the mesher's output is already in Morton order: reordering is the identity
+    assert np.array_equal(mgldg.morton_order(p, t), t)
+    rng = np.random.default_rng(7)
+    s = mgldg.morton_order(p, t[rng.permutation(len(t))])
+    assert np.array_equal(np.sort(s, axis=0), np.sort(t, axis=0))
+    assert {tuple(x) for x in s} == {tuple(x) for x in t}
+    c = p[s].mean(axis=1)
+    lo, hi = c.min(0), c.max(0)
+    q = np.minimum(np.floor((c - lo) / (hi - lo) * 2.0 ** 31), 2.0 ** 31 - 1).astype(np.uint64)
+    key = np.zeros(len(s), np.uint64)
+    for b in range(30, -1, -1):
+        for d in range(2):
+            key = (key << np.uint64(1)) | ((q[:, d] >> np.uint64(b)) & np.uint64(1))
+    assert np.all(np.diff(key.astype(np.float64)) >= 0)
+    # the LDG operator reaches two elements: its Gauss-Seidel dependency
+    # chain on the Morton-ordered disk stays far below the element count
+    pr = O.Problem.simplex(p, t, 1, 20.0, 20.0, agg_levels=1, seed=0)
+    A = pr.op(O.OP_A)
+    for rev in (False, True):
+        _, _, depth = mgldg.gs_levels(A.row_ptr, A.col_idx, rev)
+        assert depth < len(t) // 8, depth
+    with pytest.raises(mgldg.MgldgError):
+        mgldg.morton_order(p, np.full_like(t, len(p)))
