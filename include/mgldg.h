@@ -295,10 +295,12 @@ int mgldg_simplex_problem_create(mgldg_ctx* ctx, int np, const double* p, int nt
 int mgldg_simplex_problem_create_nd(mgldg_ctx* ctx, int N, int np, const double* p, int nt,
                                     const int* t, int P, double tau0, double tauD, int agg_levels,
                                     uint64_t agg_seed, mgldg_problem** out);
-/* Tetrahedra of the unit ball (no reference counterpart): the cube
- * [-1,1]^3 on an n^3 grid, n = ceil(1.4/h), Kuhn-split into six tetrahedra
- * per cube, vertices mapped onto the ball by x |x|_inf / |x|_2; p[3*np],
- * t[4*nt]; NULL arrays return the counts. */
+/* Tetrahedra of the unit ball (no reference counterpart), a cubed sphere:
+ * a core cube [-0.45,0.45]^3 of hexahedra about 2h across and radial layers
+ * of hexahedra over its faces out to the sphere, each hexahedron cut into 24
+ * tetrahedra through its face and cell centres (no tetrahedron with four
+ * vertices on the sphere), tetrahedra in Morton order; p[3*np], t[4*nt];
+ * NULL arrays return the counts. */
 int mgldg_ball_mesh(double h, int* np, int* nt, double* p, int* t);
 /* Aggregate of every element of agglomeration level l's finer mesh (agg may
  * be NULL to get the count). */

@@ -424,8 +424,9 @@ __global__ void k_bpcg_init(int k, BatchScalars sc, const double* partials, int 
     sc.delta_new[c] = d;
     sc.delta0[c] = d;
     sc.iters[c] = 0;
-    sc.broken[c] = 0;
-    sc.active[c] = (maxit > 0 && d > tol2 * d) ? 1 : 0;
+    // r.z < 0 or NaN/inf: the preconditioner is not positive definite or failed
+    sc.broken[c] = (d < 0.0 || !isfinite(d)) ? 1 : 0;
+    sc.active[c] = (maxit > 0 && d > tol2 * d && !sc.broken[c]) ? 1 : 0;
 }
 
 __global__ void k_bpcg_count(int k, BatchScalars sc) {

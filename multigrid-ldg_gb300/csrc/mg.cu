@@ -208,7 +208,8 @@ __global__ void k_pcg_init(PcgScalars* sc, const double* partials, int np) {
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sm[w];
         sc->delta_new = t;
         sc->delta0 = t;
-        sc->breakdown = t < 0.0 ? 1 : 0;   // r.z < 0: preconditioner not positive definite
+        // r.z < 0: preconditioner not positive definite; NaN/inf: it failed
+        sc->breakdown = (t < 0.0 || !isfinite(t)) ? 1 : 0;
     }
 }
 

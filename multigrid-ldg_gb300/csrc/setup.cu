@@ -307,7 +307,10 @@ static mgldg_bsr* mm(mgldg_ctx* ctx, const mgldg_bsr* X, bool tX, const mgldg_bs
 }
 
 // ------------------------------------------------------- block inverses ----
-// Gauss-Jordan with partial pivoting, one warp per block (b <= 32).
+// Gauss-Jordan with partial pivoting, one warp per block (b <= 32).  An
+// unknown whose row and column are exactly zero (a dropped coarse basis
+// function) is absent: it is eliminated as a unit diagonal and its row and
+// column of the inverse are zero (the pseudo-inverse of the block).
 __global__ void k_block_inverse(int n, int b, const double* __restrict__ val, const int* __restrict__ blk,
                                 const int* __restrict__ pos, double* __restrict__ out, int* status) {
     extern __shared__ double sm[];
@@ -326,6 +329,12 @@ __global__ void k_block_inverse(int n, int b, const double* __restrict__ val, co
             int r = q / w2, c = q - r * w2;
             aug[q] = (c < b) ? a[r * b + c] : (c - b == r ? 1.0 : 0.0);
         }
+        __syncwarp();
+        bool zero = lane < b;
+        for (int c = 0; c < b && zero; ++c) zero = aug[lane * w2 + c] == 0.0 && aug[c * w2 + lane] == 0.0;
+        const unsigned absent = __ballot_sync(0xffffffffu, zero);
+        __syncwarp();
+        if (zero) aug[lane * w2 + lane] = 1.0;
         __syncwarp();
         bool bad = false;
         for (int k = 0; k < b; ++k) {
@@ -368,7 +377,7 @@ __global__ void k_block_inverse(int n, int b, const double* __restrict__ val, co
         double* o = out + (size_t)i * b * b;
         for (int q = lane; q < b * b; q += 32) {
             int r = q / b, c = q - r * b;
-            o[q] = aug[r * w2 + b + c];
+            o[q] = ((absent >> r) & 1u) || ((absent >> c) & 1u) ? 0.0 : aug[r * w2 + b + c];
         }
         __syncwarp();
     }
@@ -700,9 +709,27 @@ __global__ void __launch_bounds__(256) k_gj_eliminate(int n, int k, double* __re
     }
 }
 
-__global__ void k_extract_right(int n, const double* aug, double* out) {
+// Absent unknowns of the dense matrix (row and column exactly zero): unit
+// diagonal for the elimination, zero rows and columns in the inverse.  One
+// warp per row; a warp writes only its own diagonal entry, after its reads.
+__global__ void k_mark_absent(int n, double* aug, int* absent) {
+    const int lane = threadIdx.x & 31;
+    const int w2 = 2 * n;
+    for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += (gridDim.x * blockDim.x) >> 5) {
+        bool z = true;
+        for (int c = lane; c < n && z; c += 32) z = aug[(size_t)r * w2 + c] == 0.0 && aug[(size_t)c * w2 + r] == 0.0;
+        z = __all_sync(0xffffffffu, z);
+        if (lane == 0) {
+            absent[r] = z ? 1 : 0;
+            if (z) aug[(size_t)r * w2 + r] = 1.0;
+        }
+    }
+}
+
+__global__ void k_extract_right(int n, const double* aug, const int* absent, double* out) {
     for (int r = blockIdx.x; r < n; r += gridDim.x)
-        for (int c = threadIdx.x; c < n; c += blockDim.x) out[(size_t)r * n + c] = aug[(size_t)r * 2 * n + n + c];
+        for (int c = threadIdx.x; c < n; c += blockDim.x)
+            out[(size_t)r * n + c] = (absent[r] || absent[c]) ? 0.0 : aug[(size_t)r * 2 * n + n + c];
 }
 
 void dense_spd_inverse(mgldg_ctx* ctx, const mgldg_bsr* A, double* out_inv) {
@@ -711,9 +738,11 @@ void dense_spd_inverse(mgldg_ctx* ctx, const mgldg_bsr* A, double* out_inv) {
     MG_REQUIRE(n <= 4096, MGLDG_ERR_UNSUPPORTED, "dense coarsest solve limited to 4096 unknowns");
     double* aug = nullptr;
     int* dstatus = nullptr;
+    int* absent = nullptr;
     try {
         aug = dalloc<double>((size_t)n * 2 * n);
         dstatus = dalloc<int>(1);
+        absent = dalloc<int>(n);
         MG_CHECK_CUDA(cudaMemsetAsync(aug, 0, (size_t)n * 2 * n * sizeof(double), ctx->stream));
         MG_CHECK_CUDA(cudaMemsetAsync(dstatus, 0, sizeof(int), ctx->stream));
         {
@@ -724,6 +753,10 @@ void dense_spd_inverse(mgldg_ctx* ctx, const mgldg_bsr* A, double* out_inv) {
         {
             Launch L(ctx, MGLDG_K_SETUP);
             k_identity_right<<<std::min(n, 1024), 256, 0, ctx->stream>>>(n, aug);
+        }
+        {
+            Launch L(ctx, MGLDG_K_SETUP);
+            k_mark_absent<<<(n + 7) / 8, 256, 0, ctx->stream>>>(n, aug, absent);
         }
         if (n <= 128) {
             Launch L(ctx, MGLDG_K_SETUP);
@@ -749,7 +782,7 @@ void dense_spd_inverse(mgldg_ctx* ctx, const mgldg_bsr* A, double* out_inv) {
         }
         {
             Launch L(ctx, MGLDG_K_SETUP);
-            k_extract_right<<<std::min(n, 1024), 256, 0, ctx->stream>>>(n, aug, out_inv);
+            k_extract_right<<<std::min(n, 1024), 256, 0, ctx->stream>>>(n, aug, absent, out_inv);
         }
         check_launch();
         int h = 0;
@@ -759,10 +792,12 @@ void dense_spd_inverse(mgldg_ctx* ctx, const mgldg_bsr* A, double* out_inv) {
     } catch (...) {
         dfree(aug);
         dfree(dstatus);
+        dfree(absent);
         throw;
     }
     dfree(aug);
     dfree(dstatus);
+    dfree(absent);
 }
 
 }  // namespace mg

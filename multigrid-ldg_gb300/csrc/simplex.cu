@@ -581,12 +581,23 @@ static void orthonormalize(const std::vector<int>& rows, std::vector<double>& va
                 G[(size_t)i * cb + j] += s;
             }
     }
+    // Cholesky G = L L^T with dropping: a column whose part M-orthogonal to
+    // the earlier kept columns has squared norm <= kDrop of its own is
+    // (numerically) in their span and is dropped -- its basis function
+    // becomes exactly zero, L(j,j) = 0 and column j of L is zero.  The tensor
+    // space interpolated at the nodes of a few simplices is rank deficient
+    // (27 functions on aggregates of tetrahedra with fewer distinct nodes);
+    // the kept columns span the same coarse space.  Row j of L keeps its
+    // entries: the dropped function's coordinates in the kept basis.
+    constexpr double kDrop = 1e-8;
     std::vector<double> L((size_t)cb * cb, 0.0);
+    std::vector<char> kept(cb, 0);
     for (int j = 0; j < cb; ++j) {
         double d = G[(size_t)j * cb + j];
         for (int k = 0; k < j; ++k) d -= L[(size_t)j * cb + k] * L[(size_t)j * cb + k];
-        const double floor = 1e-13 * G[(size_t)j * cb + j];
-        L[(size_t)j * cb + j] = std::sqrt(d > floor ? d : floor);
+        if (!(d > kDrop * G[(size_t)j * cb + j])) continue;
+        kept[j] = 1;
+        L[(size_t)j * cb + j] = std::sqrt(d);
         for (int i = j + 1; i < cb; ++i) {
             double v = G[(size_t)i * cb + j];
             for (int k = 0; k < j; ++k) v -= L[(size_t)i * cb + k] * L[(size_t)j * cb + k];
@@ -598,6 +609,10 @@ static void orthonormalize(const std::vector<int>& rows, std::vector<double>& va
         for (int r = 0; r < br; ++r) {
             double* t = T + (size_t)r * cb;
             for (int j = 0; j < cb; ++j) {
+                if (!kept[j]) {
+                    t[j] = 0.0;
+                    continue;
+                }
                 double v = t[j];
                 for (int k = 0; k < j; ++k) v -= L[(size_t)j * cb + k] * t[k];
                 t[j] = v / L[(size_t)j * cb + j];
@@ -1230,50 +1245,129 @@ static void disk_mesh(double h, std::vector<double>& p, std::vector<int>& t) {
     morton_order(2, p.data(), (int)t.size() / 3, t.data());
 }
 
-// Ball mesher (no reference counterpart): the cube [-1,1]^3 on an n^3 grid
-// (n = ceil(1.4/h)), every cube cut into the six tetrahedra of its Kuhn
-// triangulation (conforming across cubes), vertices mapped onto the ball by
-// x -> x |x|_inf / |x|_2.  Positively oriented tetrahedra, cube by cube in
-// lexicographic order.
+// Ball mesher (no reference counterpart), a cubed sphere: a core cube
+// [-a,a]^3 (a = 0.45) of m^3 hexahedra and, over each of its six faces, nr
+// radial layers of hexahedra whose vertices blend the core-surface point q
+// into q/|q| (layer l: (1 - l/nr) q + (l/nr) q/|q|).  Hexahedra are about 2h
+// across (m = ceil(a/h), nr = ceil((1-a)/(2h))).  Every hexahedron is cut
+// into 24 tetrahedra: each face into four triangles about its centre (the
+// mean of its corners, shared with the neighbour; projected onto the sphere
+// on the boundary), each triangle joined to the cell centre.  The cut of a
+// face depends only on the face, so the mesh is conforming, and no
+// tetrahedron has four vertices on the sphere (a cube grid mapped onto the
+// ball has such slivers along the cube's edges, flatter as h shrinks).
+// Positively oriented tetrahedra in the Morton order of their centroids.
 static void ball_mesh(double h, std::vector<double>& p, std::vector<int>& t) {
     MG_REQUIRE(h > 0 && h <= 2, MGLDG_ERR_ARG, "mesh size must be in (0, 2]");
-    const int n = std::max(1, (int)std::ceil(1.4 / h - 1e-12));
-    MG_REQUIRE(n <= 256, MGLDG_ERR_ARG, "mesh size too small");
-    const int m = n + 1;
+    const double a = 0.45;
+    const int m = std::max(1, (int)std::ceil(a / h - 1e-12));
+    const int nr = std::max(1, (int)std::ceil((1 - a) / (2 * h) - 1e-12));
+    MG_REQUIRE(m <= 256 && nr <= 256, MGLDG_ERR_ARG, "mesh size too small");
     p.clear();
     t.clear();
+    const int m1 = m + 1;
+    auto cid = [&](int i, int j, int k) { return (i * m1 + j) * m1 + k; };
+    for (int i = 0; i < m1; ++i)
+        for (int j = 0; j < m1; ++j)
+            for (int k = 0; k < m1; ++k) {
+                p.push_back(-a + 2 * a * i / m);
+                p.push_back(-a + 2 * a * j / m);
+                p.push_back(-a + 2 * a * k / m);
+            }
+    // shell vertex of core-surface vertex c at layer l (l = 0: c itself)
+    std::vector<int> sid((size_t)m1 * m1 * m1 * nr, -1);
+    auto shell = [&](int c, int l) {
+        if (l == 0) return c;
+        int& v = sid[(size_t)c * nr + l - 1];
+        if (v < 0) {
+            const double q[3] = {p[3 * c], p[3 * c + 1], p[3 * c + 2]};
+            const double r = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+            const double s = (double)l / nr;
+            v = (int)p.size() / 3;
+            for (int d = 0; d < 3; ++d) p.push_back(l == nr ? q[d] / r : (1 - s) * q[d] + s * q[d] / r);
+        }
+        return v;
+    };
+    // hexahedra, corners indexed x + 2y + 4z in a local frame
+    std::vector<std::array<int, 8>> hex;
     for (int i = 0; i < m; ++i)
         for (int j = 0; j < m; ++j)
             for (int k = 0; k < m; ++k) {
-                double x[3] = {-1 + 2.0 * i / n, -1 + 2.0 * j / n, -1 + 2.0 * k / n};
-                const double inf = std::max(std::fabs(x[0]), std::max(std::fabs(x[1]), std::fabs(x[2])));
-                const double two = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
-                const double s = two > 0 ? inf / two : 0.0;
-                for (int d = 0; d < 3; ++d) p.push_back(x[d] * s);
+                std::array<int, 8> hx;
+                for (int c = 0; c < 8; ++c) hx[c] = cid(i + (c & 1), j + ((c >> 1) & 1), k + ((c >> 2) & 1));
+                hex.push_back(hx);
             }
-    auto vid = [&](int i, int j, int k) { return (i * m + j) * m + k; };
-    const int perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
-    for (int i = 0; i < n; ++i)
-        for (int j = 0; j < n; ++j)
-            for (int k = 0; k < n; ++k)
-                for (auto& pm : perm) {
-                    int c[3] = {i, j, k};
-                    int v[4];
-                    v[0] = vid(c[0], c[1], c[2]);
-                    for (int s = 0; s < 3; ++s) {
-                        c[pm[s]] += 1;
-                        v[s + 1] = vid(c[0], c[1], c[2]);
+    for (int d = 0; d < 3; ++d)
+        for (int side = 0; side < 2; ++side) {
+            const int d1 = (d + 1) % 3, d2 = (d + 2) % 3;
+            for (int u = 0; u < m; ++u)
+                for (int v = 0; v < m; ++v)
+                    for (int l = 0; l < nr; ++l) {
+                        std::array<int, 8> hx;
+                        for (int c = 0; c < 8; ++c) {
+                            int ix[3];
+                            ix[d] = side ? m : 0;
+                            ix[d1] = u + (c & 1);
+                            ix[d2] = v + ((c >> 1) & 1);
+                            hx[c] = shell(cid(ix[0], ix[1], ix[2]), l + ((c >> 2) & 1));
+                        }
+                        hex.push_back(hx);
                     }
-                    // orient positively
-                    double a[3][3];
-                    for (int s = 0; s < 3; ++s)
-                        for (int d = 0; d < 3; ++d) a[s][d] = p[3 * v[s + 1] + d] - p[3 * v[0] + d];
-                    const double det = a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) -
-                                       a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]) +
-                                       a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
-                    if (det < 0) std::swap(v[2], v[3]);
-                    for (int s = 0; s < 4; ++s) t.push_back(v[s]);
+        }
+    // the 24-tetrahedron cut
+    static const int face[6][4] = {{0, 2, 6, 4}, {1, 3, 7, 5}, {0, 1, 5, 4}, {2, 3, 7, 6}, {0, 1, 3, 2}, {4, 5, 7, 6}};
+    std::map<std::array<int, 4>, int> fcen;
+    std::map<std::array<int, 4>, int> fuse;
+    for (const auto& hx : hex)
+        for (const auto& f : face) {
+            std::array<int, 4> key = {hx[f[0]], hx[f[1]], hx[f[2]], hx[f[3]]};
+            std::sort(key.begin(), key.end());
+            fuse[key]++;
+        }
+    auto push_tet = [&](int v0, int v1, int v2, int v3) {
+        double e[3][3];
+        const int w[3] = {v1, v2, v3};
+        for (int s2 = 0; s2 < 3; ++s2)
+            for (int q = 0; q < 3; ++q) e[s2][q] = p[3 * w[s2] + q] - p[3 * v0 + q];
+        const double det = e[0][0] * (e[1][1] * e[2][2] - e[1][2] * e[2][1]) -
+                           e[0][1] * (e[1][0] * e[2][2] - e[1][2] * e[2][0]) +
+                           e[0][2] * (e[1][0] * e[2][1] - e[1][1] * e[2][0]);
+        if (det < 0) std::swap(v2, v3);
+        t.push_back(v0);
+        t.push_back(v1);
+        t.push_back(v2);
+        t.push_back(v3);
+    };
+    for (const auto& hx : hex) {
+        double cc[3] = {0, 0, 0};
+        for (int c = 0; c < 8; ++c)
+            for (int q = 0; q < 3; ++q) cc[q] += p[3 * hx[c] + q] / 8;
+        const int cv = (int)p.size() / 3;
+        for (int q = 0; q < 3; ++q) p.push_back(cc[q]);
+        for (const auto& f : face) {
+            std::array<int, 4> key = {hx[f[0]], hx[f[1]], hx[f[2]], hx[f[3]]};
+            std::sort(key.begin(), key.end());
+            auto it = fcen.find(key);
+            int fv;
+            if (it != fcen.end()) {
+                fv = it->second;
+            } else {
+                double fc[3] = {0, 0, 0};
+                for (int c = 0; c < 4; ++c)
+                    for (int q = 0; q < 3; ++q) fc[q] += p[3 * hx[f[c]] + q] / 4;
+                if (fuse[key] == 1) {
+                    // a face of one hexahedron only: on the sphere
+                    const double r = std::sqrt(fc[0] * fc[0] + fc[1] * fc[1] + fc[2] * fc[2]);
+                    for (int q = 0; q < 3; ++q) fc[q] /= r;
                 }
+                fv = (int)p.size() / 3;
+                for (int q = 0; q < 3; ++q) p.push_back(fc[q]);
+                fcen.emplace(key, fv);
+            }
+            for (int c = 0; c < 4; ++c) push_tet(hx[f[c]], hx[f[(c + 1) % 4]], fv, cv);
+        }
+    }
+    morton_order(3, p.data(), (int)t.size() / 4, t.data());
 }
 
 }  // namespace mg

@@ -97,17 +97,29 @@ static Mat identity(int n) {
 // LDL^T with symmetric diagonal pivoting: P A P^T = L D L^T.  At step k the
 // largest remaining Schur-complement diagonal entry (in magnitude) is swapped
 // into position k.  Stands in for Eigen::LDLT (multigrid.h:93-95,133-135,
-// 168-170; ldgpoisson.h:25).
+// 168-170; ldgpoisson.h:25).  Extension: an unknown whose row and column are
+// exactly zero (a dropped coarse basis function) is absent -- it is factored
+// as a unit diagonal and its solution entry is zero (the pseudo-inverse).
 struct LDLT {
     int n = 0;
     std::vector<double> L;   // unit lower triangle, row-major n x n
     std::vector<double> D;
     std::vector<int> tr;     // transposition applied at step k
+    std::vector<char> absent;
     LDLT() {}
     explicit LDLT(const Mat& A) { factor(A); }
     void factor(const Mat& A) {
         n = A.r;
         std::vector<double> W(A.a);
+        absent.assign(n, 0);
+        for (int i = 0; i < n; ++i) {
+            bool z = true;
+            for (int j = 0; j < n && z; ++j) z = W[(size_t)i * n + j] == 0.0 && W[(size_t)j * n + i] == 0.0;
+            if (z) {
+                absent[i] = 1;
+                W[(size_t)i * n + i] = 1.0;
+            }
+        }
         tr.assign(n, 0);
         D.assign(n, 0.0);
         for (int k = 0; k < n; ++k) {
@@ -158,6 +170,8 @@ struct LDLT {
         }
         for (int k = n - 1; k >= 0; --k)
             if (tr[k] != k) std::swap(x[k], x[tr[k]]);
+        for (int i = 0; i < n; ++i)
+            if (absent[i]) x[i] = 0.0;
     }
     std::vector<double> solve(const double* b) const {
         std::vector<double> x(b, b + n);
@@ -1233,6 +1247,7 @@ struct Level {
     int npl = 0;
     // dense Cholesky of the whole level matrix (coarsest-level extension)
     std::vector<double> chol;
+    std::vector<char> absent;   // unknowns with zero rows and columns (dense solve)
     int nchol = 0;
 };
 
@@ -1310,6 +1325,17 @@ struct MG {
             for (int r = 0; r < b; ++r)
                 for (int c = 0; c < b; ++c)
                     D[(size_t)(kv.first.i * b + r) * n + kv.first.j * b + c] = kv.second(r, c);
+        // unknowns with exactly zero rows and columns are absent (unit
+        // diagonal, zero solution), as in LDLT
+        L.absent.assign(n, 0);
+        for (int i = 0; i < n; ++i) {
+            bool z = true;
+            for (int j = 0; j < n && z; ++j) z = D[(size_t)i * n + j] == 0.0 && D[(size_t)j * n + i] == 0.0;
+            if (z) {
+                L.absent[i] = 1;
+                D[(size_t)i * n + i] = 1.0;
+            }
+        }
         for (int j = 0; j < n; ++j) {
             double s = D[(size_t)j * n + j];
             for (int k = 0; k < j; ++k) s -= D[(size_t)j * n + k] * D[(size_t)j * n + k];
@@ -1392,6 +1418,8 @@ struct MG {
                 for (int k = i + 1; k < n; ++k) s -= L.chol[(size_t)k * n + i] * y[k];
                 y[i] = s / L.chol[(size_t)i * n + i];
             }
+            for (int i = 0; i < n; ++i)
+                if (L.absent[i]) y[i] = 0.0;
             L.x = y;
         } else {
             throw std::invalid_argument("Unknown coarse solver.");

@@ -12,6 +12,7 @@ import oracle_py as O
 
 mgldg = pytest.importorskip("mgldg")
 spla = pytest.importorskip("scipy.sparse.linalg")
+sp = pytest.importorskip("scipy.sparse")
 import adjoint_ref as R  # noqa: E402
 
 
@@ -156,7 +157,7 @@ def test_oracle_reproduces_the_ball_solution():
     # with N = 3); P2 holds it exactly, so the error is the polyhedral boundary's
     _lib_or_skip()
     errs = []
-    for h in (0.5, 0.35, 0.25):
+    for h in (0.5, 0.35):
         p, t = mgldg.ball_mesh(h)
         pr = O.Problem.simplex(p, t, 3, 1 / h, 1 / h, agg_levels=1, seed=0)
         A = R.to_scipy(pr.op(O.OP_A)).tocsc()
@@ -167,7 +168,7 @@ def test_oracle_reproduces_the_ball_solution():
         J = np.stack([p[t[:, k]] - P0 for k in (1, 2, 3)], axis=2)
         X = (P0[:, None, :] + np.einsum("eij,qj->eqi", J, nodes)).reshape(-1, 3)
         errs.append(np.abs(u - (1 - (X ** 2).sum(1)) / 6).max())
-    assert errs[-1] < errs[0] / 2.5
+    assert errs[0] < 0.06 and errs[-1] < errs[0] / 2.2
 
 
 def test_morton_order_is_a_stable_permutation_and_keeps_gauss_seidel_chains_short():
@@ -196,3 +197,39 @@ def test_morton_order_is_a_stable_permutation_and_keeps_gauss_seidel_chains_shor
         assert depth < len(t) // 8, depth
     with pytest.raises(mgldg.MgldgError):
         mgldg.morton_order(p, np.full_like(t, len(p)))
+
+
+def test_tetrahedral_coarse_bases_drop_dependent_directions():
+    # the tensor Q2 space interpolated at the P2 nodes of a few tetrahedra is
+    # rank deficient; dependent directions become exact zero columns, the
+    # kept ones are mass-orthonormal, and the V-cycle over the result is a
+    # working preconditioner
+    _lib_or_skip()
+    p, t = mgldg.ball_mesh(0.1)
+    pr = O.Problem.simplex(p, t, 3, 1 / 0.1, 1 / 0.1, agg_levels=6, agg_seed=5000, seed=4001)
+    H = pr.hierarchy()
+    M = R.to_scipy(pr.op(O.OP_M))
+    T0 = R.to_scipy(H[0])
+    G = (T0.T @ M @ T0).tocsr()
+    d = G.diagonal()
+    off = G - sp.diags(d)
+    assert (abs(off).max() if off.nnz else 0.0) <= 1e-6
+    assert np.all((np.abs(d - 1) <= 1e-6) | (d == 0))
+    zero_cols = np.flatnonzero(abs(T0).sum(axis=0).A1 == 0)
+    assert len(zero_cols) > 0 and np.array_equal(zero_cols, np.flatnonzero(d == 0))
+    for Tl in H:
+        assert np.abs(Tl.vals).max() <= 1e4
+    # constants stay in the coarse space: on each aggregate they are
+    # M-orthogonal to nothing dropped, so the M-projection of 1 reproduces 1
+    one = np.ones(T0.shape[0])
+    assert np.abs(T0 @ (T0.T @ (M @ one)) - one).max() <= 1e-6
+    p, t = mgldg.ball_mesh(0.2)
+    pr = O.Problem.simplex(p, t, 3, 1 / 0.2, 1 / 0.2, agg_levels=6, agg_seed=5000, seed=4001)
+    b = pr.rhs()
+    for relax, omega, its in ((O.RELAX_GS, 1.0, 40), (O.RELAX_JACOBI, 0.4, 75)):
+        mg = O.Multigrid(pr, relaxation=relax, omega=omega, npre=2, npost=2, solver=O.COARSE_DENSE,
+                         restriction=O.RESTRICT_RAT, mean_project=False)
+        x, hist, _ = pr.pcg(b, mg=mg, tol=1e-10, maxit=200)
+        assert len(hist) < its, (relax, len(hist))
+        A = R.to_scipy(pr.op(O.OP_A))
+        assert np.linalg.norm(b - A @ x) <= 1e-9 * np.linalg.norm(b)

@@ -69,13 +69,20 @@ def test_tet_hierarchy_rhs_and_dump_match_oracle(ctx, tmp_path):
     assert open(tmp_path / "ours.fun").read() == open(tmp_path / "ref.fun").read()
 
 
-@pytest.mark.parametrize("relax", [mgldg.RELAX_JACOBI, mgldg.RELAX_GAUSS_SEIDEL])
-def test_tet_pcg_history_matches_oracle(ctx, relax):
-    # damped block Jacobi needs omega ~ 0.3 on the 3-D agglomerated levels
-    # (with 0.7 the V-cycle stops being positive definite on finer balls)
-    p, t, prob, pr = make(ctx, 0.3, 3)
+@pytest.mark.parametrize("h,relax", [(0.3, mgldg.RELAX_JACOBI), (0.3, mgldg.RELAX_GAUSS_SEIDEL),
+                                     (0.1, mgldg.RELAX_GAUSS_SEIDEL)])
+def test_tet_pcg_history_matches_oracle(ctx, h, relax):
+    # on the 0.1 ball some aggregates' tensor spaces are rank deficient: the
+    # dropped directions are zero columns of T0 and absent unknowns of the
+    # coarse levels (zero rows in the block and dense inverses) on both sides
+    p, t, prob, pr = make(ctx, h, 3)
+    if h < 0.2:
+        _, ci, v0 = prob.T[0].download()
+        zero = np.ones((ci.max() + 1, v0.shape[2]), bool)
+        np.logical_and.at(zero, ci, np.all(v0 == 0, axis=1))
+        assert zero.any()
     b = pr.rhs()
-    omega = 0.3 if relax == mgldg.RELAX_JACOBI else 0.8
+    omega = 0.7 if relax == mgldg.RELAX_JACOBI else 0.8
     omg = O.Multigrid(pr, relaxation=relax, omega=omega, npre=2, npost=2, solver=O.COARSE_DENSE,
                       restriction=O.RESTRICT_RAT, mean_project=False)
     xr, hr, _ = pr.pcg(b, mg=omg, tol=1e-10)
@@ -133,12 +140,13 @@ def test_tet_adjoint_finite_differences_on_gpu(ctx):
 
 
 def test_indefinite_preconditioner_is_reported(ctx):
-    # on a 0.2 ball, damped Jacobi with omega 0.7 diverges on an agglomerated
-    # level; pcg must report a breakdown instead of stopping on a spurious
-    # r.z test (the solve with block Gauss-Seidel converges)
+    # block Jacobi damped by omega 1.6 is not a convergent smoother (omega
+    # exceeds 2 / lambda_max(D^-1 A)), so the V-cycle is indefinite; pcg must
+    # report a breakdown instead of stopping on a spurious r.z test (the solve
+    # with block Gauss-Seidel converges)
     p, t, prob, pr = make(ctx, 0.2, 3)
     b = pr.rhs()
-    bad = mgldg.Multigrid(ctx, prob.ops, prob.T, relaxation=mgldg.RELAX_JACOBI, omega=0.7, npre=2, npost=2,
+    bad = mgldg.Multigrid(ctx, prob.ops, prob.T, relaxation=mgldg.RELAX_JACOBI, omega=1.6, npre=2, npost=2,
                           solver=mgldg.COARSE_DENSE, restriction=mgldg.RESTRICT_RAT, mean_project=0)
     with pytest.raises(mgldg.MgldgError) as e:
         mgldg.pcg(ctx, prob.ops.A, b, precon=bad, tol=1e-10, maxit=200)
