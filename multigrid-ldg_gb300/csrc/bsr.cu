@@ -324,6 +324,56 @@ __global__ void __launch_bounds__(WPB * 32, 2)
     }
 }
 
+// Small square blocks (B <= 10): one lane per scalar row, 32 / B block rows
+// per warp (rows_dot); the same epilogue and CTA partials as k_spmv.
+template <class T, int B, int MAXB>
+__global__ void __launch_bounds__(256)
+    k_spmv_rows(int nbr, const int* __restrict__ row_ptr, const int* __restrict__ col_idx,
+                const T* __restrict__ val, const int* __restrict__ blk, T alpha, const T* __restrict__ x, T beta,
+                const T* yin, T* y, const T* dotv, int self_dot, double* __restrict__ partials) {
+    constexpr int G = Rows<B>::G;
+    __shared__ double sm[8];
+    const int lane = threadIdx.x & 31;
+    const int g = lane / B, r = lane - g * B;
+    double dacc = 0;
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    for (int base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * G; base < nbr; base += nw * G) {
+        const int row = base + g;
+        if (g < G && row < nbr) {
+            const int k0 = __ldg(row_ptr + row), k1 = __ldg(row_ptr + row + 1);
+            const T acc = rows_dot<T, B, MAXB>(col_idx, val, blk, x, k0, k1, r);
+            const size_t o = (size_t)row * B + r;
+            T v = alpha * acc;
+            if (beta != T(0)) v += beta * yin[o];
+            y[o] = v;
+            if (self_dot) dacc += (double)v * (double)v;
+            else if (dotv) dacc += (double)v * (double)dotv[o];
+        }
+    }
+    if (partials) {
+        dacc = block_sum<256>(dacc, sm);
+        if (threadIdx.x == 0) partials[blockIdx.x] = dacc;
+    }
+}
+
+template <class T, int B>
+static void launch_spmv_rows(mgldg_ctx* ctx, const mgldg_bsr* A, T alpha, const T* x, T beta, const T* yin, T* y,
+                             const T* dotv, double* partials, int* npart, int kclass) {
+    constexpr int MAXB = (sizeof(T) == 4 || B <= 4) ? 4 : 2;
+    const int rows_per_cta = 8 * Rows<B>::G;
+    int grid = std::max(1, std::min((A->nbr + rows_per_cta - 1) / rows_per_cta, ctx->sm_count * 8));
+    if (partials) grid = std::min(grid, ctx->n_partials);
+    {
+        Launch L(ctx, kclass);
+        const int self_dot = (dotv != nullptr && dotv == y) ? 1 : 0;
+        k_spmv_rows<T, B, MAXB><<<grid, 256, 0, ctx->stream>>>(A->nbr, A->row_ptr, A->col_idx, bsr_vals<T>(A), A->blk,
+                                                               alpha, x, beta, yin, y, self_dot ? nullptr : dotv,
+                                                               self_dot, partials);
+    }
+    check_launch();
+    if (npart) *npart = grid;
+}
+
 // Any block shape: one thread per output row entry.
 template <class T>
 __global__ void __launch_bounds__(256)
@@ -457,6 +507,18 @@ void spmv(mgldg_ctx* ctx, const mgldg_bsr* A, T alpha, const T* x, T beta, const
         MG_TRANSFER_CASE(25)
 #undef MG_TRANSFER_CASE
     }
+#define MG_SPMV_ROWS_CASE(R)                                                                           \
+    if (br == R && bc == R) {                                                                          \
+        launch_spmv_rows<T, R>(ctx, A, alpha, x, beta, yin, y, dotv, partials, npart, kclass);         \
+        return;                                                                                        \
+    }
+    MG_SPMV_ROWS_CASE(3)
+    MG_SPMV_ROWS_CASE(4)
+    MG_SPMV_ROWS_CASE(6)
+    MG_SPMV_ROWS_CASE(8)
+    MG_SPMV_ROWS_CASE(9)
+    MG_SPMV_ROWS_CASE(10)
+#undef MG_SPMV_ROWS_CASE
 #define MG_SPMV_CASE(R, Cc)                                                                            \
     if (br == R && bc == Cc) {                                                                         \
         launch_spmv<T, R, Cc>(ctx, A, alpha, x, beta, yin, y, dotv, partials, npart, kclass);          \

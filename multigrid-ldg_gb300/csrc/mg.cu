@@ -42,39 +42,22 @@ static void convert(mgldg_ctx* ctx, int64_t n, const A* a, B* b) {
     check_launch();
 }
 
-// coarsest level: b -= mean(b) (optional); x = Cinv b in FP64 (one CTA)
+// coarsest level: x = Cinv b in FP64, one warp per row over all SMs (each
+// CTA stages b in shared memory; Cinv, at most 128 MB, stays L2-resident
+// across V-cycles when it fits).  The optional b -= mean(b) runs first in
+// k_mean_project.
 template <class T>
-__global__ void __launch_bounds__(1024) k_coarse_solve(int n, T* b, T* x, const double* __restrict__ Cinv, int mean_project) {
+__global__ void __launch_bounds__(256) k_coarse_solve(int n, const T* __restrict__ b, T* __restrict__ x,
+                                                      const double* __restrict__ Cinv) {
     extern __shared__ double sb[];
-    __shared__ double red[32];
-    double s = 0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double v = (double)b[i];
-        sb[i] = v;
-        s += v;
-    }
-    if (mean_project) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double t = 0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
-            red[0] = t / n;
-        }
-        __syncthreads();
-        const double mean = red[0];
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            sb[i] -= mean;
-            b[i] = (T)sb[i];
-        }
-    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) sb[i] = (double)b[i];
     __syncthreads();
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int row = w; row < n; row += nw) {
+    const int lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    for (int row = blockIdx.x * wpb + (threadIdx.x >> 5); row < n; row += gridDim.x * wpb) {
+        const double* cr = Cinv + (size_t)row * n;
         double a = 0;
-        for (int c = lane; c < n; c += 32) a += Cinv[(size_t)row * n + c] * sb[c];
+        for (int c = lane; c < n; c += 32) a += cr[c] * sb[c];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
         if (lane == 0) x[row] = (T)a;
@@ -131,10 +114,15 @@ static void coarse_solve(mgldg_mg* m, int i) {
         relax<T>(m, i, m->p.npost, true);
         return;
     }
-    {
+    if (m->p.mean_project) {
         Launch K(ctx, MGLDG_K_COARSE);
-        k_coarse_solve<T><<<1, 1024, L.n * sizeof(double), ctx->stream>>>((int)L.n, LV<T>::b(L), LV<T>::x(L), m->Cinv,
-                                                                          m->p.mean_project);
+        k_mean_project<T><<<1, 1024, 0, ctx->stream>>>((int)L.n, LV<T>::b(L));
+    }
+    {
+        const int n = (int)L.n;
+        const int grid = std::max(1, std::min((n + 7) / 8, ctx->sm_count * 8));
+        Launch K(ctx, MGLDG_K_COARSE);
+        k_coarse_solve<T><<<grid, 256, L.n * sizeof(double), ctx->stream>>>(n, LV<T>::b(L), LV<T>::x(L), m->Cinv);
     }
     check_launch();
 }

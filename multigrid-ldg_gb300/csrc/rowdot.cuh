@@ -153,4 +153,51 @@ __device__ __forceinline__ T row_product(const int* __restrict__ col_idx, const 
     else return row_dot_lean<T, BR, BC>(col_idx, val, blk, x, k0, k1, r, c0, active);
 }
 
+// ---------------------------------------------------------- small blocks --
+// Blocks of B <= 10: one lane per scalar row, 32 / B block rows per warp.
+// A warp's block rows are consecutive, so their blocks form one contiguous
+// run of the value array; each lane reads its B-value row of every block
+// (the B lanes of a block row together read the whole block) and the B
+// entries of x_j shared with its group (one L1 line for the group).  MAXB
+// blocks of a row are loaded before their arithmetic.
+template <int B>
+struct Rows {
+    static constexpr int G = 32 / B;   // block rows per warp
+};
+
+template <class T, int B, int MAXB>
+__device__ __forceinline__ T rows_dot(const int* __restrict__ col_idx, const T* __restrict__ val,
+                                      const int* __restrict__ blk, const T* __restrict__ x, int k0, int k1, int r) {
+    T acc = 0;
+    for (int kb = k0; kb < k1; kb += MAXB) {
+        const int nb = min(MAXB, k1 - kb);
+        T a[MAXB][B], xv[MAXB][B];
+        int j[MAXB];
+#pragma unroll
+        for (int q = 0; q < MAXB; ++q)
+            if (q < nb) {
+                const int bq = blk ? __ldg(blk + kb + q) : kb + q;
+                const T* ap = val + ((size_t)bq * B + r) * B;
+#pragma unroll
+                for (int c = 0; c < B; ++c) a[q][c] = __ldg(ap + c);
+            }
+#pragma unroll
+        for (int q = 0; q < MAXB; ++q) j[q] = (q < nb) ? __ldg(col_idx + kb + q) : 0;
+#pragma unroll
+        for (int q = 0; q < MAXB; ++q)
+            if (q < nb) {
+                const T* xp = x + (size_t)j[q] * B;
+#pragma unroll
+                for (int c = 0; c < B; ++c) xv[q][c] = __ldg(xp + c);
+            }
+#pragma unroll
+        for (int q = 0; q < MAXB; ++q)
+            if (q < nb) {
+#pragma unroll
+                for (int c = 0; c < B; ++c) acc = fma(a[q][c], xv[q][c], acc);
+            }
+    }
+    return acc;
+}
+
 }  // namespace mg

@@ -228,6 +228,58 @@ __global__ void __launch_bounds__(WPB * 32, 2)
     }
 }
 
+// Small blocks (B <= 10): one lane per scalar row, 32 / B block rows per
+// warp (rows_dot); t = b_i - (A x_in)_i, then y = Dinv_i t with t's entries
+// shuffled within the block row's lane group.  The row loop is warp-uniform
+// so every lane takes part in the shuffles.
+template <class T, int B, int MAXB>
+__global__ void __launch_bounds__(256)
+    k_jacobi_rows(int n, const int* __restrict__ row_ptr, const int* __restrict__ col_idx, const T* __restrict__ val,
+                  const T* __restrict__ Dinv, const T* __restrict__ b, const T* __restrict__ xin, T* __restrict__ xout,
+                  T omega) {
+    constexpr int G = Rows<B>::G;
+    const int lane = threadIdx.x & 31;
+    const int g = lane / B, r = lane - g * B;
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    for (int base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * G; base < n; base += nw * G) {
+        const int row = base + g;
+        const bool valid = g < G && row < n;
+        const size_t o = (size_t)row * B + r;
+        T t = 0, xi = 0;
+        T dr[B];
+        if (valid) {
+            const T* Di = Dinv + ((size_t)row * B + r) * B;
+#pragma unroll
+            for (int c = 0; c < B; ++c) dr[c] = __ldg(Di + c);
+            xi = __ldg(xin + o);
+            const int k0 = __ldg(row_ptr + row), k1 = __ldg(row_ptr + row + 1);
+            t = __ldg(b + o) - rows_dot<T, B, MAXB>(col_idx, val, nullptr, xin, k0, k1, r);
+        }
+        T y = 0;
+        const int src = (g < G ? g : 0) * B;
+#pragma unroll
+        for (int c = 0; c < B; ++c) {
+            const T tc = __shfl_sync(0xffffffffu, t, src + c);
+            if (valid) y = fma(dr[c], tc, y);
+        }
+        if (valid) xout[o] = xi + omega * y;
+    }
+}
+
+template <class T, int B>
+static void launch_jacobi_rows(mgldg_ctx* ctx, const mgldg_bsr* A, const T* vals, const T* Dinv, const T* b,
+                               const T* xin, T* xout, T omega) {
+    constexpr int MAXB = (sizeof(T) == 4 || B <= 4) ? 4 : 2;
+    const int rows_per_cta = 8 * Rows<B>::G;
+    const int grid = std::max(1, std::min((A->nbr + rows_per_cta - 1) / rows_per_cta, ctx->sm_count * 8));
+    {
+        Launch L(ctx, MGLDG_K_JACOBI);
+        k_jacobi_rows<T, B, MAXB><<<grid, 256, 0, ctx->stream>>>(A->nbr, A->row_ptr, A->col_idx, vals, Dinv, b, xin,
+                                                                 xout, omega);
+    }
+    check_launch();
+}
+
 // -------------------------------------------------------------- scheduling --
 // Level sets of one sweep direction (dir 0: rows ascending, 1: descending).
 // A row depends on its earlier neighbours in the symmetrised pattern (an
@@ -400,6 +452,14 @@ void jacobi_sweep(mgldg_ctx* ctx, const mgldg_bsr* A, const T* vals, const T* Di
     if constexpr (std::is_same<T, float>::value) {
         if (bulk_jacobi_f32(ctx, A, vals, Dinv, b, xin, xout, omega)) return;
     }
+    if (!A->blk) switch (A->br) {
+            case 3: launch_jacobi_rows<T, 3>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
+            case 4: launch_jacobi_rows<T, 4>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
+            case 6: launch_jacobi_rows<T, 6>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
+            case 8: launch_jacobi_rows<T, 8>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
+            case 9: launch_jacobi_rows<T, 9>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
+            case 10: launch_jacobi_rows<T, 10>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
+        }
     switch (A->br) {
         case 1: launch_jacobi<T, 1>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
         case 3: launch_jacobi<T, 3>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
