@@ -324,26 +324,33 @@ __global__ void __launch_bounds__(WPB * 32, 2)
     }
 }
 
-// Small square blocks (B <= 10): one lane per scalar row, 32 / B block rows
-// per warp (rows_dot); the same epilogue and CTA partials as k_spmv.
+// Small square blocks (B <= 10): 32 / B block rows per warp, one lane per
+// block column (cols_accumulate, rows_reduce); the same epilogue and CTA
+// partials as k_spmv.
 template <class T, int B, int MAXB>
 __global__ void __launch_bounds__(256)
     k_spmv_rows(int nbr, const int* __restrict__ row_ptr, const int* __restrict__ col_idx,
                 const T* __restrict__ val, const int* __restrict__ blk, T alpha, const T* __restrict__ x, T beta,
                 const T* yin, T* y, const T* dotv, int self_dot, double* __restrict__ partials) {
-    constexpr int G = Rows<B>::G;
+    using R = Rows<B>;
+    __shared__ T sr[8 * R::SM];
     __shared__ double sm[8];
-    const int lane = threadIdx.x & 31;
-    const int g = lane / B, r = lane - g * B;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane / B, c = lane - g * B;
+    T* s = sr + warp * R::SM;
     double dacc = 0;
     const int nw = gridDim.x * (blockDim.x >> 5);
-    for (int base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * G; base < nbr; base += nw * G) {
+    for (int base = (blockIdx.x * (blockDim.x >> 5) + warp) * R::G; base < nbr; base += nw * R::G) {
         const int row = base + g;
-        if (g < G && row < nbr) {
-            const int k0 = __ldg(row_ptr + row), k1 = __ldg(row_ptr + row + 1);
-            const T acc = rows_dot<T, B, MAXB>(col_idx, val, blk, x, k0, k1, r);
-            const size_t o = (size_t)row * B + r;
-            T v = alpha * acc;
+        const bool valid = g < R::G && row < nbr;
+        T acc[B];
+#pragma unroll
+        for (int r = 0; r < B; ++r) acc[r] = 0;
+        if (valid) cols_accumulate<T, B, MAXB>(col_idx, val, blk, x, __ldg(row_ptr + row), __ldg(row_ptr + row + 1), c, acc);
+        const T sum = rows_reduce<T, B>(acc, s, g, c, g < R::G);
+        if (valid) {
+            const size_t o = (size_t)row * B + c;
+            T v = alpha * sum;
             if (beta != T(0)) v += beta * yin[o];
             y[o] = v;
             if (self_dot) dacc += (double)v * (double)v;

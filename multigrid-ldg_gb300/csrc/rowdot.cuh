@@ -154,50 +154,67 @@ __device__ __forceinline__ T row_product(const int* __restrict__ col_idx, const 
 }
 
 // ---------------------------------------------------------- small blocks --
-// Blocks of B <= 10: one lane per scalar row, 32 / B block rows per warp.
-// A warp's block rows are consecutive, so their blocks form one contiguous
-// run of the value array; each lane reads its B-value row of every block
-// (the B lanes of a block row together read the whole block) and the B
-// entries of x_j shared with its group (one L1 line for the group).  MAXB
-// blocks of a row are loaded before their arithmetic.
+// Blocks of B <= 10, 32 / B block rows per warp, lane (g, c) owning column c
+// of the warp's g-th block row.  For every block the lane reads column c of
+// each block row r -- a[r][c], the B lanes of a group together one
+// contiguous B-value row per load -- and its single entry x_j[c], and keeps
+// B partial sums acc[r].  The warp's block rows are consecutive, so their
+// blocks are one contiguous run of the value array.  rows_reduce then sums
+// acc[r] over the group's lanes through shared memory, in column order, and
+// leaves row r's total on lane (g, r).
 template <int B>
 struct Rows {
-    static constexpr int G = 32 / B;   // block rows per warp
+    static constexpr int G = 32 / B;        // block rows per warp
+    static constexpr int LD = B + 1;        // padded shared-memory row
+    static constexpr int SM = G * B * LD;   // values per warp
 };
 
 template <class T, int B, int MAXB>
-__device__ __forceinline__ T rows_dot(const int* __restrict__ col_idx, const T* __restrict__ val,
-                                      const int* __restrict__ blk, const T* __restrict__ x, int k0, int k1, int r) {
-    T acc = 0;
+__device__ __forceinline__ void cols_accumulate(const int* __restrict__ col_idx, const T* __restrict__ val,
+                                                const int* __restrict__ blk, const T* __restrict__ x, int k0, int k1,
+                                                int c, T (&acc)[B]) {
     for (int kb = k0; kb < k1; kb += MAXB) {
         const int nb = min(MAXB, k1 - kb);
-        T a[MAXB][B], xv[MAXB][B];
+        T a[MAXB][B], xv[MAXB];
         int j[MAXB];
-#pragma unroll
-        for (int q = 0; q < MAXB; ++q)
-            if (q < nb) {
-                const int bq = blk ? __ldg(blk + kb + q) : kb + q;
-                const T* ap = val + ((size_t)bq * B + r) * B;
-#pragma unroll
-                for (int c = 0; c < B; ++c) a[q][c] = __ldg(ap + c);
-            }
 #pragma unroll
         for (int q = 0; q < MAXB; ++q) j[q] = (q < nb) ? __ldg(col_idx + kb + q) : 0;
 #pragma unroll
         for (int q = 0; q < MAXB; ++q)
             if (q < nb) {
-                const T* xp = x + (size_t)j[q] * B;
+                const int bq = blk ? __ldg(blk + kb + q) : kb + q;
+                const T* ap = val + (size_t)bq * (B * B) + c;
 #pragma unroll
-                for (int c = 0; c < B; ++c) xv[q][c] = __ldg(xp + c);
+                for (int r = 0; r < B; ++r) a[q][r] = __ldg(ap + r * B);
             }
+#pragma unroll
+        for (int q = 0; q < MAXB; ++q) xv[q] = (q < nb) ? __ldg(x + (size_t)j[q] * B + c) : T(0);
 #pragma unroll
         for (int q = 0; q < MAXB; ++q)
             if (q < nb) {
 #pragma unroll
-                for (int c = 0; c < B; ++c) acc = fma(a[q][c], xv[q][c], acc);
+                for (int r = 0; r < B; ++r) acc[r] = fma(a[q][r], xv[q], acc[r]);
             }
     }
-    return acc;
+}
+
+// Sum of acc[r] over the lanes of group g, returned on lane (g, r); `s` is
+// the warp's Rows<B>::SM values of shared memory.  All lanes must call it.
+template <class T, int B>
+__device__ __forceinline__ T rows_reduce(const T (&acc)[B], T* s, int g, int c, bool in_group) {
+    using R = Rows<B>;
+    if (in_group) {
+#pragma unroll
+        for (int r = 0; r < B; ++r) s[(g * B + r) * R::LD + c] = acc[r];
+    }
+    __syncwarp();
+    T y = 0;
+    if (in_group) {
+#pragma unroll
+        for (int cc = 0; cc < B; ++cc) y += s[(g * B + c) * R::LD + cc];
+    }
+    __syncwarp();
+    return y;
 }
 
 }  // namespace mg

@@ -228,39 +228,45 @@ __global__ void __launch_bounds__(WPB * 32, 2)
     }
 }
 
-// Small blocks (B <= 10): one lane per scalar row, 32 / B block rows per
-// warp (rows_dot); t = b_i - (A x_in)_i, then y = Dinv_i t with t's entries
-// shuffled within the block row's lane group.  The row loop is warp-uniform
-// so every lane takes part in the shuffles.
+// Small blocks (B <= 10): 32 / B block rows per warp, one lane per block
+// column for the product (cols_accumulate, rows_reduce), then lane (g, r)
+// holds t_r = b_r - (A x_in)_r and applies row r of Dinv with t's entries
+// shuffled within the group.  The row loop is warp-uniform so every lane
+// takes part in the shuffles and the shared-memory reduction.
 template <class T, int B, int MAXB>
 __global__ void __launch_bounds__(256)
     k_jacobi_rows(int n, const int* __restrict__ row_ptr, const int* __restrict__ col_idx, const T* __restrict__ val,
                   const T* __restrict__ Dinv, const T* __restrict__ b, const T* __restrict__ xin, T* __restrict__ xout,
                   T omega) {
-    constexpr int G = Rows<B>::G;
-    const int lane = threadIdx.x & 31;
-    const int g = lane / B, r = lane - g * B;
+    using R = Rows<B>;
+    __shared__ T sr[8 * R::SM];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane / B, c = lane - g * B;
+    T* s = sr + warp * R::SM;
     const int nw = gridDim.x * (blockDim.x >> 5);
-    for (int base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * G; base < n; base += nw * G) {
+    for (int base = (blockIdx.x * (blockDim.x >> 5) + warp) * R::G; base < n; base += nw * R::G) {
         const int row = base + g;
-        const bool valid = g < G && row < n;
-        const size_t o = (size_t)row * B + r;
-        T t = 0, xi = 0;
-        T dr[B];
+        const bool valid = g < R::G && row < n;
+        const size_t o = (size_t)row * B + c;
+        T acc[B];
+#pragma unroll
+        for (int r = 0; r < B; ++r) acc[r] = 0;
+        T bi = 0, xi = 0;
         if (valid) {
-            const T* Di = Dinv + ((size_t)row * B + r) * B;
-#pragma unroll
-            for (int c = 0; c < B; ++c) dr[c] = __ldg(Di + c);
+            bi = __ldg(b + o);
             xi = __ldg(xin + o);
-            const int k0 = __ldg(row_ptr + row), k1 = __ldg(row_ptr + row + 1);
-            t = __ldg(b + o) - rows_dot<T, B, MAXB>(col_idx, val, nullptr, xin, k0, k1, r);
+            cols_accumulate<T, B, MAXB>(col_idx, val, nullptr, xin, __ldg(row_ptr + row), __ldg(row_ptr + row + 1), c,
+                                        acc);
         }
+        const T t = bi - rows_reduce<T, B>(acc, s, g, c, g < R::G);
+        // lane (g, c) now holds t_c; y_c = sum_k Dinv(c, k) t_k
+        const T* Di = Dinv + ((size_t)row * B + c) * B;
+        const int src = (g < R::G ? g : 0) * B;
         T y = 0;
-        const int src = (g < G ? g : 0) * B;
 #pragma unroll
-        for (int c = 0; c < B; ++c) {
-            const T tc = __shfl_sync(0xffffffffu, t, src + c);
-            if (valid) y = fma(dr[c], tc, y);
+        for (int k = 0; k < B; ++k) {
+            const T tk = __shfl_sync(0xffffffffu, t, src + k);
+            if (valid) y = fma(__ldg(Di + k), tk, y);
         }
         if (valid) xout[o] = xi + omega * y;
     }
