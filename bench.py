@@ -394,7 +394,8 @@ def run_unstructured(args, ctx, ext, torch, local, ws):
     bs = b.cpu().numpy()
     res1 = float(np.linalg.norm(A.mv(xs, alpha=-1.0, beta=1.0, y=bs)) / np.linalg.norm(bs))
     out["single"] = {
-        "workload": (f"unit disk, ring mesh h={h}: {prob.ne:,} triangles, P2 LDG (6 DOF/element, {prob.ndof:,} "
+        "workload": (f"unit disk, ring mesh h={h} in Morton order: {prob.ne:,} triangles, P2 LDG (6 DOF/element, "
+                     f"{prob.ndof:,} "
                      f"DOF), tau=1/h, {nlev} agglomeration levels (dense coarsest), mixed precision, Jacobi "
                      f"omega=0.7, V(2,2), tol 1e-10"),
         "ms_per_solve": ms, "iters": iters, "true_rel_residual": res1, "problem_build_ms": build_ms,
@@ -402,6 +403,8 @@ def run_unstructured(args, ctx, ext, torch, local, ws):
     }
     del mg, prob, b, x
     torch.cuda.empty_cache()
+    if args.disk_batch <= 0:
+        return out
 
     # ---- uneven batch of meshes ----
     rng = np.random.default_rng(4000)
@@ -735,7 +738,7 @@ def run_gpu(args, ws, rank, local):
     del mgs
     if args.batched > 0:
         batched = run_batched(args, ctx, ext, torch, local, ws)
-    unstructured = run_unstructured(args, ctx, ext, torch, local, ws) if args.disk_batch > 0 else None
+    unstructured = run_unstructured(args, ctx, ext, torch, local, ws) if args.disk_h > 0 else None
     adjoint = run_adjoint(args, ctx, ext, torch, local, ws) if args.ball_h > 0 else None
 
     speedup = {}
@@ -788,7 +791,8 @@ def main():
     ap.add_argument("--batched", type=int, default=64, help="right-hand sides of the multi-RHS line (0: skip)")
     ap.add_argument("--batched-n", type=int, default=512, help="mesh side of the uniform multi-RHS mesh")
     ap.add_argument("--batched-mesh", default="adaptive", choices=["adaptive", "uniform"])
-    ap.add_argument("--disk-h", type=float, default=0.004, help="mesh size of the single unstructured disk")
+    ap.add_argument("--disk-h", type=float, default=0.004, help="mesh size of the single unstructured disk (0: skip "
+                    "the unstructured lines)")
     ap.add_argument("--disk-batch", type=int, default=48, help="meshes in the uneven batch (0: skip the line)")
     ap.add_argument("--ball-h", type=float, default=0.026, help="tetrahedral ball mesh size of the adjoint line (0: skip)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
