@@ -324,32 +324,36 @@ __global__ void __launch_bounds__(WPB * 32, 2)
     }
 }
 
-// Small square blocks (B <= 10): 32 / B block rows per warp, one lane per
+// Small square blocks (3..10): 32 / B block rows per warp, one lane per
 // block column (cols_accumulate, rows_reduce); the same epilogue and CTA
-// partials as k_spmv.
-template <class T, int B, int MAXB>
+// partials as k_spmv.  (The transfers' rectangular blocks, 6x9 and 9x6 on
+// triangles, ran slower this way than one thread per output entry: one
+// block per prolongation row leaves the reduction unamortised.)
+template <class T, int BR, int BC, int MAXB>
 __global__ void __launch_bounds__(256)
     k_spmv_rows(int nbr, const int* __restrict__ row_ptr, const int* __restrict__ col_idx,
                 const T* __restrict__ val, const int* __restrict__ blk, T alpha, const T* __restrict__ x, T beta,
                 const T* yin, T* y, const T* dotv, int self_dot, double* __restrict__ partials) {
-    using R = Rows<B>;
+    using R = Rows<BR, BC>;
     __shared__ T sr[8 * R::SM];
     __shared__ double sm[8];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int g = lane / B, c = lane - g * B;
+    const int g = lane / R::S, c = lane - g * R::S;
     T* s = sr + warp * R::SM;
     double dacc = 0;
     const int nw = gridDim.x * (blockDim.x >> 5);
     for (int base = (blockIdx.x * (blockDim.x >> 5) + warp) * R::G; base < nbr; base += nw * R::G) {
         const int row = base + g;
         const bool valid = g < R::G && row < nbr;
-        T acc[B];
+        T acc[BR];
 #pragma unroll
-        for (int r = 0; r < B; ++r) acc[r] = 0;
-        if (valid) cols_accumulate<T, B, MAXB>(col_idx, val, blk, x, __ldg(row_ptr + row), __ldg(row_ptr + row + 1), c, acc);
-        const T sum = rows_reduce<T, B>(acc, s, g, c, g < R::G);
-        if (valid) {
-            const size_t o = (size_t)row * B + c;
+        for (int r = 0; r < BR; ++r) acc[r] = 0;
+        if (valid && c < BC)
+            cols_accumulate<T, BR, BC, MAXB>(col_idx, val, blk, x, __ldg(row_ptr + row), __ldg(row_ptr + row + 1), c,
+                                             acc);
+        const T sum = rows_reduce<T, BR, BC>(acc, s, g, c, g < R::G);
+        if (valid && c < BR) {
+            const size_t o = (size_t)row * BR + c;
             T v = alpha * sum;
             if (beta != T(0)) v += beta * yin[o];
             y[o] = v;
@@ -363,19 +367,20 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-template <class T, int B>
+template <class T, int BR, int BC>
 static void launch_spmv_rows(mgldg_ctx* ctx, const mgldg_bsr* A, T alpha, const T* x, T beta, const T* yin, T* y,
                              const T* dotv, double* partials, int* npart, int kclass) {
-    constexpr int MAXB = (sizeof(T) == 4 || B <= 4) ? 4 : 2;
-    const int rows_per_cta = 8 * Rows<B>::G;
+    constexpr int B = BR > BC ? BR : BC;
+    constexpr int MAXB = sizeof(T) == 4 ? (BR <= 10 ? 4 : 2) : (B <= 4 ? 4 : (BR <= 10 ? 2 : 1));
+    const int rows_per_cta = 8 * Rows<BR, BC>::G;
     int grid = std::max(1, std::min((A->nbr + rows_per_cta - 1) / rows_per_cta, ctx->sm_count * 8));
     if (partials) grid = std::min(grid, ctx->n_partials);
     {
         Launch L(ctx, kclass);
         const int self_dot = (dotv != nullptr && dotv == y) ? 1 : 0;
-        k_spmv_rows<T, B, MAXB><<<grid, 256, 0, ctx->stream>>>(A->nbr, A->row_ptr, A->col_idx, bsr_vals<T>(A), A->blk,
-                                                               alpha, x, beta, yin, y, self_dot ? nullptr : dotv,
-                                                               self_dot, partials);
+        k_spmv_rows<T, BR, BC, MAXB><<<grid, 256, 0, ctx->stream>>>(A->nbr, A->row_ptr, A->col_idx, bsr_vals<T>(A),
+                                                                    A->blk, alpha, x, beta, yin, y,
+                                                                    self_dot ? nullptr : dotv, self_dot, partials);
     }
     check_launch();
     if (npart) *npart = grid;
@@ -514,17 +519,17 @@ void spmv(mgldg_ctx* ctx, const mgldg_bsr* A, T alpha, const T* x, T beta, const
         MG_TRANSFER_CASE(25)
 #undef MG_TRANSFER_CASE
     }
-#define MG_SPMV_ROWS_CASE(R)                                                                           \
-    if (br == R && bc == R) {                                                                          \
-        launch_spmv_rows<T, R>(ctx, A, alpha, x, beta, yin, y, dotv, partials, npart, kclass);         \
+#define MG_SPMV_ROWS_CASE(R, Cc)                                                                       \
+    if (br == R && bc == Cc) {                                                                         \
+        launch_spmv_rows<T, R, Cc>(ctx, A, alpha, x, beta, yin, y, dotv, partials, npart, kclass);     \
         return;                                                                                        \
     }
-    MG_SPMV_ROWS_CASE(3)
-    MG_SPMV_ROWS_CASE(4)
-    MG_SPMV_ROWS_CASE(6)
-    MG_SPMV_ROWS_CASE(8)
-    MG_SPMV_ROWS_CASE(9)
-    MG_SPMV_ROWS_CASE(10)
+    MG_SPMV_ROWS_CASE(3, 3)
+    MG_SPMV_ROWS_CASE(4, 4)
+    MG_SPMV_ROWS_CASE(6, 6)
+    MG_SPMV_ROWS_CASE(8, 8)
+    MG_SPMV_ROWS_CASE(9, 9)
+    MG_SPMV_ROWS_CASE(10, 10)
 #undef MG_SPMV_ROWS_CASE
 #define MG_SPMV_CASE(R, Cc)                                                                            \
     if (br == R && bc == Cc) {                                                                         \

@@ -154,28 +154,30 @@ __device__ __forceinline__ T row_product(const int* __restrict__ col_idx, const 
 }
 
 // ---------------------------------------------------------- small blocks --
-// Blocks of B <= 10, 32 / B block rows per warp, lane (g, c) owning column c
-// of the warp's g-th block row.  For every block the lane reads column c of
-// each block row r -- a[r][c], the B lanes of a group together one
-// contiguous B-value row per load -- and its single entry x_j[c], and keeps
-// B partial sums acc[r].  The warp's block rows are consecutive, so their
-// blocks are one contiguous run of the value array.  rows_reduce then sums
-// acc[r] over the group's lanes through shared memory, in column order, and
-// leaves row r's total on lane (g, r).
-template <int B>
+// Blocks of BR x BC with max(BR, BC) <= 32 (used for square 3..10): lane
+// groups of S = max(BR, BC) lanes, 32 / S block rows per warp, lane (g, c) owning
+// column c (< BC) of the warp's g-th block row.  For every block the lane
+// reads column c of each block row r -- a[r][c], the group's lanes together
+// one contiguous BC-value row per load -- and its single entry x_j[c], and
+// keeps BR partial sums acc[r].  The warp's block rows are consecutive, so
+// their blocks are one contiguous run of the value array.  rows_reduce then
+// sums acc[r] over the group's lanes through shared memory, in column
+// order, and leaves row r's total on lane (g, r) (r < BR).
+template <int BR, int BC = BR>
 struct Rows {
-    static constexpr int G = 32 / B;        // block rows per warp
-    static constexpr int LD = B + 1;        // padded shared-memory row
-    static constexpr int SM = G * B * LD;   // values per warp
+    static constexpr int S = BR > BC ? BR : BC;   // lanes per block row
+    static constexpr int G = 32 / S;              // block rows per warp
+    static constexpr int LD = BC + 1;             // padded shared-memory row
+    static constexpr int SM = G * BR * LD;        // values per warp
 };
 
-template <class T, int B, int MAXB>
+template <class T, int BR, int BC, int MAXB>
 __device__ __forceinline__ void cols_accumulate(const int* __restrict__ col_idx, const T* __restrict__ val,
                                                 const int* __restrict__ blk, const T* __restrict__ x, int k0, int k1,
-                                                int c, T (&acc)[B]) {
+                                                int c, T (&acc)[BR]) {
     for (int kb = k0; kb < k1; kb += MAXB) {
         const int nb = min(MAXB, k1 - kb);
-        T a[MAXB][B], xv[MAXB];
+        T a[MAXB][BR], xv[MAXB];
         int j[MAXB];
 #pragma unroll
         for (int q = 0; q < MAXB; ++q) j[q] = (q < nb) ? __ldg(col_idx + kb + q) : 0;
@@ -183,35 +185,36 @@ __device__ __forceinline__ void cols_accumulate(const int* __restrict__ col_idx,
         for (int q = 0; q < MAXB; ++q)
             if (q < nb) {
                 const int bq = blk ? __ldg(blk + kb + q) : kb + q;
-                const T* ap = val + (size_t)bq * (B * B) + c;
+                const T* ap = val + (size_t)bq * (BR * BC) + c;
 #pragma unroll
-                for (int r = 0; r < B; ++r) a[q][r] = __ldg(ap + r * B);
+                for (int r = 0; r < BR; ++r) a[q][r] = __ldg(ap + r * BC);
             }
 #pragma unroll
-        for (int q = 0; q < MAXB; ++q) xv[q] = (q < nb) ? __ldg(x + (size_t)j[q] * B + c) : T(0);
+        for (int q = 0; q < MAXB; ++q) xv[q] = (q < nb) ? __ldg(x + (size_t)j[q] * BC + c) : T(0);
 #pragma unroll
         for (int q = 0; q < MAXB; ++q)
             if (q < nb) {
 #pragma unroll
-                for (int r = 0; r < B; ++r) acc[r] = fma(a[q][r], xv[q], acc[r]);
+                for (int r = 0; r < BR; ++r) acc[r] = fma(a[q][r], xv[q], acc[r]);
             }
     }
 }
 
-// Sum of acc[r] over the lanes of group g, returned on lane (g, r); `s` is
-// the warp's Rows<B>::SM values of shared memory.  All lanes must call it.
-template <class T, int B>
-__device__ __forceinline__ T rows_reduce(const T (&acc)[B], T* s, int g, int c, bool in_group) {
-    using R = Rows<B>;
-    if (in_group) {
+// Sum of acc[r] over the group's lanes c < BC, returned on lane (g, r) for
+// r < BR (0 elsewhere); `s` is the warp's Rows<BR, BC>::SM values of shared
+// memory.  All lanes must call it.
+template <class T, int BR, int BC>
+__device__ __forceinline__ T rows_reduce(const T (&acc)[BR], T* s, int g, int c, bool in_group) {
+    using R = Rows<BR, BC>;
+    if (in_group && c < BC) {
 #pragma unroll
-        for (int r = 0; r < B; ++r) s[(g * B + r) * R::LD + c] = acc[r];
+        for (int r = 0; r < BR; ++r) s[(g * BR + r) * R::LD + c] = acc[r];
     }
     __syncwarp();
     T y = 0;
-    if (in_group) {
+    if (in_group && c < BR) {
 #pragma unroll
-        for (int cc = 0; cc < B; ++cc) y += s[(g * B + c) * R::LD + cc];
+        for (int cc = 0; cc < BC; ++cc) y += s[(g * BR + c) * R::LD + cc];
     }
     __syncwarp();
     return y;

@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(256)
     using R = Rows<B>;
     __shared__ T sr[8 * R::SM];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int g = lane / B, c = lane - g * B;
+    const int g = lane / R::S, c = lane - g * R::S;
     T* s = sr + warp * R::SM;
     const int nw = gridDim.x * (blockDim.x >> 5);
     for (int base = (blockIdx.x * (blockDim.x >> 5) + warp) * R::G; base < n; base += nw * R::G) {
@@ -255,10 +255,10 @@ __global__ void __launch_bounds__(256)
         if (valid) {
             bi = __ldg(b + o);
             xi = __ldg(xin + o);
-            cols_accumulate<T, B, MAXB>(col_idx, val, nullptr, xin, __ldg(row_ptr + row), __ldg(row_ptr + row + 1), c,
-                                        acc);
+            cols_accumulate<T, B, B, MAXB>(col_idx, val, nullptr, xin, __ldg(row_ptr + row), __ldg(row_ptr + row + 1),
+                                           c, acc);
         }
-        const T t = bi - rows_reduce<T, B>(acc, s, g, c, g < R::G);
+        const T t = bi - rows_reduce<T, B, B>(acc, s, g, c, g < R::G);
         // lane (g, c) now holds t_c; y_c = sum_k Dinv(c, k) t_k
         const T* Di = Dinv + ((size_t)row * B + c) * B;
         const int src = (g < R::G ? g : 0) * B;
