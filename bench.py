@@ -159,29 +159,36 @@ def cpu_baseline(n, P, levels, iters, tol, seed):
 
 
 # ------------------------------------------------------------- GPU forms --
-def level_bytes(mg, nlev, s):
-    """Per level: algorithmic bytes of one GS sweep, one Jacobi sweep, one SpMV."""
+def level_bytes(mg, nlev, s, f16=False):
+    """Per level: algorithmic bytes of one GS sweep, one Jacobi sweep, one SpMV.
+    f16: the level operator is read from its block-scaled FP16 copy (2 bytes
+    per entry + one 4-byte scale per block; inverse diagonal blocks and
+    vectors in FP32, s = 4)."""
     out = []
     for l in range(nlev):
         nbr, nbc, br, bc, nnzb = mg.level_op(l, 4).info()
         b2 = br * bc
         n = nbr * br
         idx = 4 * nnzb + 4 * (nbr + 1)
+        av = nnzb * (b2 * 2 + 4) if f16 else nnzb * b2 * s
         gs = (nnzb - nbr) * b2 * s + nbr * b2 * s + idx + 3 * n * s
-        jac = nnzb * b2 * s + nbr * b2 * s + idx + 3 * n * s
-        spmv = nnzb * b2 * s + idx + 3 * n * s
+        jac = av + nbr * b2 * s + idx + 3 * n * s
+        spmv = av + idx + 3 * n * s
         out.append(dict(gs=gs, jacobi=jac, spmv=spmv, nbr=nbr, nnzb=nnzb, b=br))
     return out
 
 
 FORMS = {
     # name: (relaxation, omega, precision) -- MGLDG_RELAX_* / MGLDG_PREC_* values
+    "mixed16_jacobi": (0, 0.7, 2),
     "mixed_jacobi": (0, 0.7, 1),
     "fp64_jacobi": (0, 0.7, 0),
     "mixed_gs": (1, 0.8, 1),
     "fp64_gs": (1, 0.8, 0),
 }
-FORM_TEXT = {"mixed_jacobi": "mixed precision, damped block Jacobi omega=0.7",
+FORM_TEXT = {"mixed16_jacobi": ("mixed precision with the level operators stored as block-scaled FP16 (one FP32 "
+                               "scale per block), damped block Jacobi omega=0.7"),
+             "mixed_jacobi": "mixed precision, damped block Jacobi omega=0.7",
              "fp64_jacobi": "FP64, damped block Jacobi omega=0.7",
              "mixed_gs": "mixed precision, block Gauss-Seidel omega=0.8",
              "fp64_gs": "FP64, block Gauss-Seidel omega=0.8"}
@@ -371,7 +378,7 @@ def run_unstructured(args, ctx, ext, torch, local, ws):
     nlev = _coarse_levels(prob)
     t0 = time.perf_counter()
     mg = mgldg.Multigrid(ctx, prob.ops, prob.T, npre=2, npost=2, solver=mgldg.COARSE_DENSE, max_levels=nlev,
-                         mean_project=0, relaxation=mgldg.RELAX_JACOBI, omega=0.7, precision=mgldg.PREC_MIXED)
+                         mean_project=0, relaxation=mgldg.RELAX_JACOBI, omega=0.7, precision=_vprec(args))
     setup_ms = (time.perf_counter() - t0) * 1e3
     b = torch.empty(prob.ndof, dtype=torch.float64, device=dev)
     x = torch.zeros_like(b)
@@ -396,7 +403,7 @@ def run_unstructured(args, ctx, ext, torch, local, ws):
     out["single"] = {
         "workload": (f"unit disk, ring mesh h={h} in Morton order: {prob.ne:,} triangles, P2 LDG (6 DOF/element, "
                      f"{prob.ndof:,} "
-                     f"DOF), tau=1/h, {nlev} agglomeration levels (dense coarsest), mixed precision, Jacobi "
+                     f"DOF), tau=1/h, {nlev} agglomeration levels (dense coarsest), {_vtext(args)}, Jacobi "
                      f"omega=0.7, V(2,2), tol 1e-10"),
         "ms_per_solve": ms, "iters": iters, "true_rel_residual": res1, "problem_build_ms": build_ms,
         "mg_setup_ms": setup_ms,
@@ -417,7 +424,7 @@ def run_unstructured(args, ctx, ext, torch, local, ws):
     build_ms = (time.perf_counter() - t0) * 1e3
     nlev = _coarse_levels(prob)
     mg = mgldg.Multigrid(ctx, prob.ops, prob.T, npre=2, npost=2, solver=mgldg.COARSE_DENSE, max_levels=nlev,
-                         mean_project=0, relaxation=mgldg.RELAX_JACOBI, omega=0.7, precision=mgldg.PREC_MIXED)
+                         mean_project=0, relaxation=mgldg.RELAX_JACOBI, omega=0.7, precision=_vprec(args))
     off = (eoff * prob.npl).astype(np.int64)
     nseg = len(meshes)
     b = torch.empty(prob.ndof, dtype=torch.float64, device=dev)
@@ -450,7 +457,7 @@ def run_unstructured(args, ctx, ext, torch, local, ws):
         "workload": (f"{nseg} disks, h ~ U[0.01,0.04] (seed 4000), {prob.ne:,} triangles / {prob.ndof:,} DOF in "
                      f"total ({min(len(t) for _, t in meshes):,}..{max(len(t) for _, t in meshes):,} per mesh), "
                      f"one block-diagonal union, segmented PCG (per-mesh CG scalars and stopping), {nlev} "
-                     f"agglomeration levels, mixed precision, Jacobi omega=0.7, V(2,2), tol 1e-10 per mesh"),
+                     f"agglomeration levels, {_vtext(args)}, Jacobi omega=0.7, V(2,2), tol 1e-10 per mesh"),
         "ms_per_batch": ms, "meshes_per_s": nseg / (ms * 1e-3), "iters_min": int(it.min()), "iters_max": int(it.max()),
         "worst_true_rel_residual": worst,
         "problem_build_ms": build_ms,
@@ -458,6 +465,17 @@ def run_unstructured(args, ctx, ext, torch, local, ws):
     del mg, prob, b, x, tmp
     torch.cuda.empty_cache()
     return out
+
+
+def _vprec(args):
+    """V-cycle precision of the unstructured and adjoint lines."""
+    import mgldg
+    return mgldg.PREC_MIXED_F16 if args.vcycle == "mixed16" else mgldg.PREC_MIXED
+
+
+def _vtext(args):
+    return ("mixed precision with FP16-stored level operators (one FP32 scale per block)" if args.vcycle == "mixed16"
+            else "mixed precision")
 
 
 def _field_at(X, seed, corr=0.2, sigma=0.5, nfeat=64):
@@ -492,7 +510,7 @@ def run_adjoint(args, ctx, ext, torch, local, ws):
     nlev = _coarse_levels(prob)
     kw = dict(npre=2, npost=2, solver=mgldg.COARSE_DENSE, max_levels=nlev, mean_project=0,
               relaxation=mgldg.RELAX_JACOBI, omega=0.7, restriction=mgldg.RESTRICT_RAT,
-              precision=mgldg.PREC_MIXED)
+              precision=_vprec(args))
     n, ne = prob.ndof, prob.ne
     b = torch.empty(n, dtype=torch.float64, device=dev)
     u = torch.zeros_like(b)
@@ -551,7 +569,7 @@ def run_adjoint(args, ctx, ext, torch, local, ws):
                      f"P2 LDG (10 DOF/element, "
                      f"{n:,} DOF), kappa_e = exp(g_e) (random-Fourier-feature field, corr 0.2, sigma 0.5, seed 5011), "
                      f"u_obs from kappa seed 5012, L = 1/2 ||u - u_obs||^2; forward + adjoint MG-PCG on one hierarchy "
-                     f"({nlev} agglomeration levels, RAT, dense coarsest), mixed precision, block Jacobi "
+                     f"({nlev} agglomeration levels, RAT, dense coarsest), {_vtext(args)}, block Jacobi "
                      f"omega=0.7, V(2,2), "
                      f"tol 1e-10, plus dL/dkappa"),
         "ms_per_gradient": ms, "forward_iters": int(itp[0]), "adjoint_iters": int(itp[1]),
@@ -693,8 +711,8 @@ def run_gpu(args, ws, rank, local):
     # library's stream in the profiled pass of the same steps.
     relax_h, _, prec_h = FORMS[headline]
     prof, per_level = profs[headline]
-    s = 4 if prec_h == 1 else 8
-    lb = level_bytes(mgs[headline], levels - 1, s)
+    s = 4 if prec_h in (1, 2) else 8
+    lb = level_bytes(mgs[headline], levels - 1, s, f16=prec_h == 2)
     cls = max(prof, key=lambda k: prof[k][1])
     key = {"gauss_seidel": "gs", "jacobi": "jacobi", "spmv": "spmv"}.get(cls)
     roof = {"bound": "hbm", "kernel": cls, "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None,
@@ -712,6 +730,12 @@ def run_gpu(args, ws, rank, local):
             # algorithmic bytes; profiles/k_rows_bulk_jacobi_fp32_256x256_q3.md),
             # scaled to this launch by its algorithmic bytes
             roof["traffic"] = bytes0 * (418.508032 / 415.756292)
+            roof["traffic_source"] = "ncu at 256x256 Q3, scaled by block rows"
+        if headline == "mixed16_jacobi" and key == "jacobi":
+            # the same for the FP16-copy kernel: 253.668352 MB of DRAM
+            # traffic for 249.815044 MB of algorithmic bytes at 256x256 Q3
+            # (profiles/k_rows_bulk_jacobi_f16_256x256_q3.md)
+            roof["traffic"] = bytes0 * (253.668352 / 249.815044)
             roof["traffic_source"] = "ncu at 256x256 Q3, scaled by block rows"
     gpu_launches = int(sum(v[0] for v in prof.values()))
     results[headline]["per_level_ms"] = {k: {str(l): round(v[1] / args.steps, 4) for l, v in d.items()}
@@ -745,6 +769,8 @@ def run_gpu(args, ws, rank, local):
     for sm in ("gs", "jacobi"):
         if f"fp64_{sm}" in results and f"mixed_{sm}" in results:
             speedup[sm] = results[f"fp64_{sm}"]["ms"] / results[f"mixed_{sm}"]["ms"]
+    if "fp64_jacobi" in results and "mixed16_jacobi" in results:
+        speedup["jacobi_f16"] = results["fp64_jacobi"]["ms"] / results["mixed16_jacobi"]["ms"]
     f64 = [results[f]["ms"] for f in results if f.startswith("fp64")]
     mx = [results[f]["ms"] for f in results if f.startswith("mixed")]
     if f64 and mx:
@@ -754,7 +780,7 @@ def run_gpu(args, ws, rank, local):
         "metric": METRIC, "value": results[headline]["ms"], "unit": "ms", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": results[headline]["ms"], "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 V-cycle / f64 CG" if prec_h == 1 else "f64",
+        "dtype": {1: "f32 V-cycle / f64 CG", 2: "f16-stored level operators, f32 V-cycle / f64 CG"}.get(prec_h, "f64"),
         "data": f"synthetic: seeded 8-Gaussian forcing (seed {WL['seed']}), homogeneous Dirichlet",
         "config": {"workload": workload_name(n, P, levels), "form": FORM_TEXT[headline],
                    "parallelism": "replicas" if ws > 1 else "single GPU",
@@ -786,8 +812,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=WL["n"])
     ap.add_argument("--levels", type=int, default=WL["levels"])
-    ap.add_argument("--forms", default="mixed_jacobi,fp64_jacobi,mixed_gs,fp64_gs")
-    ap.add_argument("--headline", default="mixed_jacobi")
+    ap.add_argument("--forms", default="mixed16_jacobi,mixed_jacobi,fp64_jacobi,mixed_gs,fp64_gs")
+    ap.add_argument("--headline", default="mixed16_jacobi")
     ap.add_argument("--batched", type=int, default=64, help="right-hand sides of the multi-RHS line (0: skip)")
     ap.add_argument("--batched-n", type=int, default=512, help="mesh side of the uniform multi-RHS mesh")
     ap.add_argument("--batched-mesh", default="adaptive", choices=["adaptive", "uniform"])
@@ -796,6 +822,8 @@ def main():
     ap.add_argument("--disk-batch", type=int, default=48, help="meshes in the uneven batch (0: skip the line)")
     ap.add_argument("--ball-h", type=float, default=0.026, help="tetrahedral ball mesh size of the adjoint line (0: skip)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
+    ap.add_argument("--vcycle", default="mixed16", choices=["mixed16", "mixed"],
+                    help="V-cycle form of the unstructured and adjoint lines")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":

@@ -121,6 +121,9 @@ int mgldg_ops_destroy(mgldg_ops* ops);
 #define MGLDG_RESTRICT_RATRAT    1   /* MG::kRATRAT */
 #define MGLDG_PREC_FP64          0   /* plain form: FP64 throughout */
 #define MGLDG_PREC_MIXED         1   /* FP32 V-cycle, FP64 coarsest solve (and FP64 pcg) */
+#define MGLDG_PREC_MIXED_F16     2   /* MIXED, with the level operators' Jacobi sweeps and
+                                        residuals reading a block-scaled FP16 copy (one FP32
+                                        scale per block) for square blocks 3..10 and 16 */
 
 /* MG::Parameters (multigrid.h:48-62) plus the build's extensions. */
 typedef struct mgldg_mg_params {

@@ -697,7 +697,7 @@ static void ensure_batch(mgldg_mg* m, int k, const mgldg_bsr* A_outer) {
         b->k = k;
         m->batch = b;
         b->L.resize(m->L.size());
-        const bool mixed = m->p.precision == MGLDG_PREC_MIXED;
+        const bool mixed = m->p.precision != MGLDG_PREC_FP64;
         for (size_t l = 0; l < m->L.size(); ++l) {
             const int64_t nk = std::max<int64_t>(1, m->L[l].n * k);
             BatchLevel& B = b->L[l];
@@ -732,7 +732,7 @@ static void ensure_batch(mgldg_mg* m, int k, const mgldg_bsr* A_outer) {
     if (!b->tuned) {
         // tile widths per level operator and kernel, on the level buffers
         // (their contents are overwritten before every use)
-        const bool mixed = m->p.precision == MGLDG_PREC_MIXED;
+        const bool mixed = m->p.precision != MGLDG_PREC_FP64;
         for (size_t l = 0; l < m->L.size(); ++l) {
             LevelData& L = m->L[l];
             BatchLevel& B = b->L[l];
@@ -891,7 +891,7 @@ static void bprecon(mgldg_mg* m, const double* R, double* S, bool x_is_zero) {
         mgldg_ctx* c;
         ~LevelReset() { c->cur_level = -1; }
     } reset{ctx};
-    if (m->p.precision == MGLDG_PREC_MIXED) {
+    if (m->p.precision != MGLDG_PREC_FP64) {
         bconvert<double, float>(ctx, nk, R, B.b32);
         if (x_is_zero) MG_CHECK_CUDA(cudaMemsetAsync(B.x32, 0, nk * sizeof(float), ctx->stream));
         else bconvert<double, float>(ctx, nk, S, B.x32);

@@ -329,11 +329,12 @@ __global__ void __launch_bounds__(WPB * 32, 2)
 // partials as k_spmv.  (The transfers' rectangular blocks, 6x9 and 9x6 on
 // triangles, ran slower this way than one thread per output entry: one
 // block per prolongation row leaves the reduction unamortised.)
-template <class T, int BR, int BC, int MAXB>
+template <class T, class VT, int BR, int BC, int MAXB>
 __global__ void __launch_bounds__(256)
     k_spmv_rows(int nbr, const int* __restrict__ row_ptr, const int* __restrict__ col_idx,
-                const T* __restrict__ val, const int* __restrict__ blk, T alpha, const T* __restrict__ x, T beta,
-                const T* yin, T* y, const T* dotv, int self_dot, double* __restrict__ partials) {
+                const VT* __restrict__ val, const float* __restrict__ scl, const int* __restrict__ blk, T alpha,
+                const T* __restrict__ x, T beta, const T* yin, T* y, const T* dotv, int self_dot,
+                double* __restrict__ partials) {
     using R = Rows<BR, BC>;
     __shared__ T sr[8 * R::SM];
     __shared__ double sm[8];
@@ -349,8 +350,8 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
         for (int r = 0; r < BR; ++r) acc[r] = 0;
         if (valid && c < BC)
-            cols_accumulate<T, BR, BC, MAXB>(col_idx, val, blk, x, __ldg(row_ptr + row), __ldg(row_ptr + row + 1), c,
-                                             acc);
+            cols_accumulate<T, VT, BR, BC, MAXB>(col_idx, val, scl, blk, x, __ldg(row_ptr + row),
+                                                 __ldg(row_ptr + row + 1), c, acc);
         const T sum = rows_reduce<T, BR, BC>(acc, s, g, c, g < R::G);
         if (valid && c < BR) {
             const size_t o = (size_t)row * BR + c;
@@ -367,9 +368,10 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-template <class T, int BR, int BC>
+template <class T, int BR, int BC, class VT = T>
 static void launch_spmv_rows(mgldg_ctx* ctx, const mgldg_bsr* A, T alpha, const T* x, T beta, const T* yin, T* y,
-                             const T* dotv, double* partials, int* npart, int kclass) {
+                             const T* dotv, double* partials, int* npart, int kclass, const VT* vals = nullptr,
+                             const float* scl = nullptr) {
     constexpr int B = BR > BC ? BR : BC;
     constexpr int MAXB = sizeof(T) == 4 ? (BR <= 10 ? 4 : 2) : (B <= 4 ? 4 : (BR <= 10 ? 2 : 1));
     const int rows_per_cta = 8 * Rows<BR, BC>::G;
@@ -378,9 +380,9 @@ static void launch_spmv_rows(mgldg_ctx* ctx, const mgldg_bsr* A, T alpha, const 
     {
         Launch L(ctx, kclass);
         const int self_dot = (dotv != nullptr && dotv == y) ? 1 : 0;
-        k_spmv_rows<T, BR, BC, MAXB><<<grid, 256, 0, ctx->stream>>>(A->nbr, A->row_ptr, A->col_idx, bsr_vals<T>(A),
-                                                                    A->blk, alpha, x, beta, yin, y,
-                                                                    self_dot ? nullptr : dotv, self_dot, partials);
+        k_spmv_rows<T, VT, BR, BC, MAXB><<<grid, 256, 0, ctx->stream>>>(
+            A->nbr, A->row_ptr, A->col_idx, vals ? vals : (const VT*)bsr_vals<T>(A), scl, A->blk, alpha, x, beta, yin,
+            y, self_dot ? nullptr : dotv, self_dot, partials);
     }
     check_launch();
     if (npart) *npart = grid;
@@ -613,6 +615,54 @@ void bsr_ensure_fp32(mgldg_bsr* A) {
     check_launch();
 }
 
+bool spmv_f16(mgldg_ctx* ctx, const mgldg_bsr* A, float alpha, const float* x, float beta, const float* yin, float* y,
+              int kclass) {
+    if (!A->val16 || A->nbr == 0 || !f16_shape(A->br, A->bc)) return false;
+    switch (A->br) {
+#define MG_F16_CASE(R)                                                                                            \
+        case R:                                                                                                   \
+            launch_spmv_rows<float, R, R, __half>(ctx, A, alpha, x, beta, yin, y, nullptr, nullptr, nullptr, kclass, \
+                                                  A->val16, A->scale16);                                          \
+            return true;
+        MG_F16_CASE(3)
+        MG_F16_CASE(4)
+        MG_F16_CASE(6)
+        MG_F16_CASE(8)
+        MG_F16_CASE(9)
+        MG_F16_CASE(10)
+#undef MG_F16_CASE
+        case 16: return bulk_spmv_f16(ctx, A, alpha, x, beta, yin, y, kclass);
+    }
+    return false;
+}
+
+// one thread per block: scale = largest magnitude, entries / scale in FP16
+__global__ void k_to_f16(int64_t nblk, int bsz, const double* __restrict__ a, __half* __restrict__ h,
+                         float* __restrict__ scale) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nblk; k += (int64_t)gridDim.x * blockDim.x) {
+        const double* ak = a + k * bsz;
+        double m = 0;
+        for (int e = 0; e < bsz; ++e) m = fmax(m, fabs(ak[e]));
+        const double s = m > 0 ? m : 1.0;
+        scale[k] = (float)s;
+        for (int e = 0; e < bsz; ++e) h[k * bsz + e] = __float2half_rn((float)(ak[e] / s));
+    }
+}
+
+void bsr_ensure_f16(mgldg_bsr* A) {
+    if (A->val16) return;
+    const int64_t nb = A->nvals_blocks();
+    A->val16 = dalloc<__half>(std::max<int64_t>(1, nb * (int64_t)A->bsz()));
+    A->scale16 = dalloc<float>(nb + 4);
+    MG_CHECK_CUDA(cudaMemsetAsync(A->scale16, 0, (nb + 4) * sizeof(float), A->ctx->stream));
+    if (nb) {
+        const int g = (int)std::min<int64_t>((nb + 255) / 256, A->ctx->sm_count * 32);
+        Launch L(A->ctx, MGLDG_K_SETUP);
+        k_to_f16<<<g, 256, 0, A->ctx->stream>>>(nb, (int)A->bsz(), A->val, A->val16, A->scale16);
+    }
+    check_launch();
+}
+
 }  // namespace mg
 
 mgldg_bsr::~mgldg_bsr() {
@@ -620,6 +670,8 @@ mgldg_bsr::~mgldg_bsr() {
     dfree(col_idx);
     dfree(val);
     dfree(val32);
+    dfree(val16);
+    dfree(scale16);
     dfree(blk);
     dfree(diag);
 }

@@ -1,6 +1,7 @@
 // internal.cuh -- shared host structures and device helpers of libmgldg.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -167,6 +168,12 @@ struct mgldg_bsr {
     int* col_idx = nullptr;
     double* val = nullptr;       // FP64 values (nnzb or nuniq blocks)
     float* val32 = nullptr;      // FP32 copy, built on demand (mixed precision)
+    // block-scaled FP16 copy (MGLDG_PREC_MIXED_F16): block k's entries are
+    // scale16[k] * val16[k * bsz() + e], scale16[k] the block's largest
+    // magnitude, so every stored half lies in [-1, 1]; scale16 has four
+    // spare entries (bulk copies move whole 16-byte words)
+    __half* val16 = nullptr;
+    float* scale16 = nullptr;
     int* blk = nullptr;          // optional block indirection
     std::vector<int> h_blk;
     int64_t nuniq = 0;
@@ -195,6 +202,17 @@ mgldg_bsr* bsr_new(mgldg_ctx* ctx, int nbr, int nbc, int br, int bc,
                    const std::vector<int>& row_ptr, const std::vector<int>& col_idx);
 void bsr_build_diag(mgldg_bsr* A);
 void bsr_ensure_fp32(mgldg_bsr* A);
+void bsr_ensure_f16(mgldg_bsr* A);
+// V-cycle products on the block-scaled FP16 copy (FP32 vectors and
+// arithmetic); false when the matrix has no such copy or the shape has no kernel
+bool spmv_f16(mgldg_ctx* ctx, const mgldg_bsr* A, float alpha, const float* x, float beta, const float* yin, float* y,
+              int kclass);
+bool jacobi_f16(mgldg_ctx* ctx, const mgldg_bsr* A, const float* Dinv, const float* b, const float* xin, float* xout,
+                float omega);
+// block sizes with FP16 kernels (square 3..10 and 16)
+inline bool f16_shape(int br, int bc) {
+    return br == bc && (br == 3 || br == 4 || br == 6 || br == 8 || br == 9 || br == 10 || br == 16);
+}
 template <class T>
 const T* bsr_vals(const mgldg_bsr* A);
 // y = alpha*A*x + beta*yin (yin may alias y or be null when beta == 0);
@@ -231,6 +249,10 @@ bool bulk_spmv_f32(mgldg_ctx* ctx, const mgldg_bsr* A, float alpha, const float*
                    float* y, int kclass);
 bool bulk_jacobi_f32(mgldg_ctx* ctx, const mgldg_bsr* A, const float* vals, const float* Dinv, const float* b,
                      const float* xin, float* xout, float omega);
+bool bulk_spmv_f16(mgldg_ctx* ctx, const mgldg_bsr* A, float alpha, const float* x, float beta, const float* yin,
+                   float* y, int kclass);
+bool bulk_jacobi_f16(mgldg_ctx* ctx, const mgldg_bsr* A, const float* Dinv, const float* b, const float* xin,
+                     float* xout, float omega);
 // reads and clears the device error word; throws MGLDG_ERR_TIMEOUT if set
 void take_device_error(mgldg_ctx* ctx);
 

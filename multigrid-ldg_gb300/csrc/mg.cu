@@ -9,7 +9,11 @@
 // keeps FP32 copies of every level operator, inverse diagonal block and
 // transfer, runs the whole V-cycle in FP32 with FP32 accumulation, and keeps
 // the coarsest solve (mean projection and dense inverse), the outer CG
-// residuals, dot products and updates in FP64.
+// residuals, dot products and updates in FP64.  MGLDG_PREC_MIXED_F16 is the
+// mixed form with the level operators' Jacobi sweeps and residuals reading a
+// block-scaled FP16 copy (one FP32 scale per block, entries / scale in FP16)
+// where the block shape has such kernels (square 3..10 and 16); everything
+// else, including the inverse diagonal blocks and the transfers, stays FP32.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -84,14 +88,34 @@ __global__ void k_mean_project(int n, T* b) {
 }
 
 // ----------------------------------------------------------------- V-cycle --
+// the FP16-copy forms of the level products (FP32 vectors only)
+template <class T>
+static bool jacobi_f16_t(mgldg_ctx*, const mgldg_bsr*, const T*, const T*, const T*, T*, T) { return false; }
+template <>
+bool jacobi_f16_t<float>(mgldg_ctx* ctx, const mgldg_bsr* A, const float* D, const float* b, const float* xin,
+                         float* xout, float omega) {
+    return jacobi_f16(ctx, A, D, b, xin, xout, omega);
+}
+template <class T>
+static bool spmv_f16_t(mgldg_ctx*, const mgldg_bsr*, T, const T*, T, const T*, T*) { return false; }
+template <>
+bool spmv_f16_t<float>(mgldg_ctx* ctx, const mgldg_bsr* A, float alpha, const float* x, float beta, const float* yin,
+                       float* y) {
+    return spmv_f16(ctx, A, alpha, x, beta, yin, y, MGLDG_K_SPMV);
+}
+
 template <class T>
 static void relax(mgldg_mg* m, int i, int n, bool reverse) {
     LevelData& L = m->L[i];
     m->ctx->cur_level = i;
     const T* vals = bsr_vals<T>(L.A);
+    const bool f16 = m->p.precision == MGLDG_PREC_MIXED_F16;
     for (int k = 0; k < n; ++k) {
         if (m->p.relaxation == MGLDG_RELAX_JACOBI) {
-            jacobi_sweep<T>(m->ctx, L.A, vals, LV<T>::D(L), LV<T>::b(L), LV<T>::x(L), LV<T>::xt(L), (T)m->p.omega);
+            if (!(f16 && jacobi_f16_t<T>(m->ctx, L.A, LV<T>::D(L), LV<T>::b(L), LV<T>::x(L), LV<T>::xt(L),
+                                          (T)m->p.omega)))
+                jacobi_sweep<T>(m->ctx, L.A, vals, LV<T>::D(L), LV<T>::b(L), LV<T>::x(L), LV<T>::xt(L),
+                                (T)m->p.omega);
             std::swap(LV<T>::x(L), LV<T>::xt(L));
         } else {
             gs_sweep<T>(m->ctx, L.A, vals, LV<T>::D(L), LV<T>::b(L), LV<T>::x(L), L.sched, (T)m->p.omega, reverse);
@@ -139,7 +163,9 @@ static void vcycle(mgldg_mg* m, int i) {
     relax<T>(m, i, m->p.npre, false);
     // r = b - A x ; b_c = T^T r ; x_c = 0
     ctx->cur_level = i;
-    spmv<T>(ctx, L.A, T(-1), LV<T>::x(L), T(1), LV<T>::b(L), LV<T>::r(L));
+    if (!(m->p.precision == MGLDG_PREC_MIXED_F16 &&
+          spmv_f16_t<T>(ctx, L.A, T(-1), LV<T>::x(L), T(1), LV<T>::b(L), LV<T>::r(L))))
+        spmv<T>(ctx, L.A, T(-1), LV<T>::x(L), T(1), LV<T>::b(L), LV<T>::r(L));
     spmv<T>(ctx, L.Tt, T(1), LV<T>::r(L), T(0), (const T*)nullptr, LV<T>::b(C), nullptr, nullptr, nullptr,
             MGLDG_K_TRANSFER);
     MG_CHECK_CUDA(cudaMemsetAsync(LV<T>::x(C), 0, C.n * sizeof(T), ctx->stream));
@@ -166,7 +192,7 @@ static void vcycle_dev(mgldg_mg* m, const double* b, double* x, bool x_is_zero) 
         mgldg_ctx* c;
         ~LevelReset() { c->cur_level = -1; }
     } reset{ctx};
-    if (m->p.precision == MGLDG_PREC_MIXED) {
+    if (m->p.precision != MGLDG_PREC_FP64) {
         convert<double, float>(ctx, L.n, b, L.b32);
         if (x_is_zero) MG_CHECK_CUDA(cudaMemsetAsync(L.x32, 0, L.n * sizeof(float), ctx->stream));
         else convert<double, float>(ctx, L.n, x, L.x32);
@@ -512,9 +538,11 @@ static void level_alloc(mgldg_ctx* ctx, mgldg_mg* m, LevelData& L, bool need_sch
         throw;
     }
     dfree(dstatus);
-    const bool mixed = m->p.precision == MGLDG_PREC_MIXED;
+    const bool mixed = m->p.precision != MGLDG_PREC_FP64;
     if (mixed) {
         bsr_ensure_fp32(const_cast<mgldg_bsr*>(L.A));
+        if (m->p.precision == MGLDG_PREC_MIXED_F16 && !L.A->blk && f16_shape(L.A->br, L.A->bc))
+            bsr_ensure_f16(const_cast<mgldg_bsr*>(L.A));
         L.Dinv32 = dalloc<float>((size_t)L.ne * L.b * L.b);
         convert<double, float>(ctx, (int64_t)L.ne * L.b * L.b, L.Dinv, L.Dinv32);
         L.x32 = dalloc<float>(L.n); L.b32 = dalloc<float>(L.n); L.r32 = dalloc<float>(L.n); L.xt32 = dalloc<float>(L.n);
@@ -539,7 +567,9 @@ extern "C" int mgldg_mg_create(mgldg_ctx* ctx, const mgldg_ops* fine, const mgld
                    p.solver == MGLDG_COARSE_DENSE, MGLDG_ERR_ARG, "Unknown coarse solver.");
     MG_REQUIRE(p.restriction == MGLDG_RESTRICT_RAT || p.restriction == MGLDG_RESTRICT_RATRAT, MGLDG_ERR_ARG,
                "Unknown restriction method.");
-    MG_REQUIRE(p.precision == MGLDG_PREC_FP64 || p.precision == MGLDG_PREC_MIXED, MGLDG_ERR_ARG, "Unknown precision.");
+    MG_REQUIRE(p.precision == MGLDG_PREC_FP64 || p.precision == MGLDG_PREC_MIXED ||
+                   p.precision == MGLDG_PREC_MIXED_F16,
+               MGLDG_ERR_ARG, "Unknown precision.");
     MG_REQUIRE(p.npre >= 0 && p.npost >= 0, MGLDG_ERR_ARG, "negative smoothing count");
     MG_REQUIRE(fine->A != nullptr, MGLDG_ERR_ARG, "fine operators lack A (call construct_laplacian)");
     mgldg_mg* m = new mgldg_mg();
@@ -578,7 +608,7 @@ extern "C" int mgldg_mg_create(mgldg_ctx* ctx, const mgldg_ops* fine, const mgld
             m->L[i + 1].ops = c;
             m->L[i + 1].owns_ops = true;
             phase("galerkin", i);
-            if (p.precision == MGLDG_PREC_MIXED) {
+            if (p.precision != MGLDG_PREC_FP64) {
                 bsr_ensure_fp32(Tc);
                 bsr_ensure_fp32(m->L[i].Tt);
             }
@@ -667,7 +697,7 @@ extern "C" int mgldg_mg_relax(mgldg_ctx* ctx, mgldg_mg* m, int level, int n, int
         dx = dalloc<double>(L.n);
         upload(ctx, db, b, L.n);
         upload(ctx, dx, x, L.n);
-        if (m->p.precision == MGLDG_PREC_MIXED) {
+        if (m->p.precision != MGLDG_PREC_FP64) {
             convert<double, float>(ctx, L.n, db, L.b32);
             convert<double, float>(ctx, L.n, dx, L.x32);
             relax<float>(m, level, n, reverse != 0);

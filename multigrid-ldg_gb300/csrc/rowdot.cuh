@@ -171,13 +171,20 @@ struct Rows {
     static constexpr int SM = G * BR * LD;        // values per warp
 };
 
-template <class T, int BR, int BC, int MAXB>
-__device__ __forceinline__ void cols_accumulate(const int* __restrict__ col_idx, const T* __restrict__ val,
-                                                const int* __restrict__ blk, const T* __restrict__ x, int k0, int k1,
-                                                int c, T (&acc)[BR]) {
+// value readers: T from the stored type (FP64, FP32 or block-scaled FP16)
+__device__ __forceinline__ double ld_val(const double* p) { return __ldg(p); }
+__device__ __forceinline__ float ld_val(const float* p) { return __ldg(p); }
+__device__ __forceinline__ float ld_val(const __half* p) { return __half2float(__ldg(p)); }
+
+// scl: per-block scales of a block-scaled FP16 matrix (null otherwise); a
+// block's scale is folded into the lane's x entry
+template <class T, class VT, int BR, int BC, int MAXB>
+__device__ __forceinline__ void cols_accumulate(const int* __restrict__ col_idx, const VT* __restrict__ val,
+                                                const float* __restrict__ scl, const int* __restrict__ blk,
+                                                const T* __restrict__ x, int k0, int k1, int c, T (&acc)[BR]) {
     for (int kb = k0; kb < k1; kb += MAXB) {
         const int nb = min(MAXB, k1 - kb);
-        T a[MAXB][BR], xv[MAXB];
+        T a[MAXB][BR], xv[MAXB], sc[MAXB];
         int j[MAXB];
 #pragma unroll
         for (int q = 0; q < MAXB; ++q) j[q] = (q < nb) ? __ldg(col_idx + kb + q) : 0;
@@ -185,12 +192,13 @@ __device__ __forceinline__ void cols_accumulate(const int* __restrict__ col_idx,
         for (int q = 0; q < MAXB; ++q)
             if (q < nb) {
                 const int bq = blk ? __ldg(blk + kb + q) : kb + q;
-                const T* ap = val + (size_t)bq * (BR * BC) + c;
+                const VT* ap = val + (size_t)bq * (BR * BC) + c;
 #pragma unroll
-                for (int r = 0; r < BR; ++r) a[q][r] = __ldg(ap + r * BC);
+                for (int r = 0; r < BR; ++r) a[q][r] = ld_val(ap + r * BC);
+                sc[q] = scl ? (T)__ldg(scl + bq) : T(1);
             }
 #pragma unroll
-        for (int q = 0; q < MAXB; ++q) xv[q] = (q < nb) ? __ldg(x + (size_t)j[q] * BC + c) : T(0);
+        for (int q = 0; q < MAXB; ++q) xv[q] = (q < nb) ? __ldg(x + (size_t)j[q] * BC + c) * sc[q] : T(0);
 #pragma unroll
         for (int q = 0; q < MAXB; ++q)
             if (q < nb) {

@@ -233,11 +233,11 @@ __global__ void __launch_bounds__(WPB * 32, 2)
 // holds t_r = b_r - (A x_in)_r and applies row r of Dinv with t's entries
 // shuffled within the group.  The row loop is warp-uniform so every lane
 // takes part in the shuffles and the shared-memory reduction.
-template <class T, int B, int MAXB>
+template <class T, class VT, int B, int MAXB>
 __global__ void __launch_bounds__(256)
-    k_jacobi_rows(int n, const int* __restrict__ row_ptr, const int* __restrict__ col_idx, const T* __restrict__ val,
-                  const T* __restrict__ Dinv, const T* __restrict__ b, const T* __restrict__ xin, T* __restrict__ xout,
-                  T omega) {
+    k_jacobi_rows(int n, const int* __restrict__ row_ptr, const int* __restrict__ col_idx, const VT* __restrict__ val,
+                  const float* __restrict__ scl, const T* __restrict__ Dinv, const T* __restrict__ b,
+                  const T* __restrict__ xin, T* __restrict__ xout, T omega) {
     using R = Rows<B>;
     __shared__ T sr[8 * R::SM];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -255,8 +255,8 @@ __global__ void __launch_bounds__(256)
         if (valid) {
             bi = __ldg(b + o);
             xi = __ldg(xin + o);
-            cols_accumulate<T, B, B, MAXB>(col_idx, val, nullptr, xin, __ldg(row_ptr + row), __ldg(row_ptr + row + 1),
-                                           c, acc);
+            cols_accumulate<T, VT, B, B, MAXB>(col_idx, val, scl, nullptr, xin, __ldg(row_ptr + row),
+                                               __ldg(row_ptr + row + 1), c, acc);
         }
         const T t = bi - rows_reduce<T, B, B>(acc, s, g, c, g < R::G);
         // lane (g, c) now holds t_c; y_c = sum_k Dinv(c, k) t_k
@@ -272,16 +272,16 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-template <class T, int B>
-static void launch_jacobi_rows(mgldg_ctx* ctx, const mgldg_bsr* A, const T* vals, const T* Dinv, const T* b,
-                               const T* xin, T* xout, T omega) {
+template <class T, int B, class VT = T>
+static void launch_jacobi_rows(mgldg_ctx* ctx, const mgldg_bsr* A, const VT* vals, const T* Dinv, const T* b,
+                               const T* xin, T* xout, T omega, const float* scl = nullptr) {
     constexpr int MAXB = (sizeof(T) == 4 || B <= 4) ? 4 : 2;
     const int rows_per_cta = 8 * Rows<B>::G;
     const int grid = std::max(1, std::min((A->nbr + rows_per_cta - 1) / rows_per_cta, ctx->sm_count * 8));
     {
         Launch L(ctx, MGLDG_K_JACOBI);
-        k_jacobi_rows<T, B, MAXB><<<grid, 256, 0, ctx->stream>>>(A->nbr, A->row_ptr, A->col_idx, vals, Dinv, b, xin,
-                                                                 xout, omega);
+        k_jacobi_rows<T, VT, B, MAXB><<<grid, 256, 0, ctx->stream>>>(A->nbr, A->row_ptr, A->col_idx, vals, scl, Dinv,
+                                                                     b, xin, xout, omega);
     }
     check_launch();
 }
@@ -480,6 +480,26 @@ void jacobi_sweep(mgldg_ctx* ctx, const mgldg_bsr* A, const T* vals, const T* Di
     }
     throw Error(MGLDG_ERR_UNSUPPORTED, "Jacobi: unsupported block size");
 }
+bool jacobi_f16(mgldg_ctx* ctx, const mgldg_bsr* A, const float* Dinv, const float* b, const float* xin, float* xout,
+                float omega) {
+    if (!A->val16 || A->blk || A->nbr == 0 || !f16_shape(A->br, A->bc)) return false;
+    switch (A->br) {
+#define MG_F16_CASE(R)                                                                                        \
+        case R:                                                                                               \
+            launch_jacobi_rows<float, R, __half>(ctx, A, A->val16, Dinv, b, xin, xout, omega, A->scale16);    \
+            return true;
+        MG_F16_CASE(3)
+        MG_F16_CASE(4)
+        MG_F16_CASE(6)
+        MG_F16_CASE(8)
+        MG_F16_CASE(9)
+        MG_F16_CASE(10)
+#undef MG_F16_CASE
+        case 16: return bulk_jacobi_f16(ctx, A, Dinv, b, xin, xout, omega);
+    }
+    return false;
+}
+
 template void jacobi_sweep<double>(mgldg_ctx*, const mgldg_bsr*, const double*, const double*, const double*,
                                    const double*, double*, double);
 template void jacobi_sweep<float>(mgldg_ctx*, const mgldg_bsr*, const float*, const float*, const float*, const float*,
