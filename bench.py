@@ -822,8 +822,9 @@ def main():
     ap.add_argument("--disk-batch", type=int, default=48, help="meshes in the uneven batch (0: skip the line)")
     ap.add_argument("--ball-h", type=float, default=0.026, help="tetrahedral ball mesh size of the adjoint line (0: skip)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
-    ap.add_argument("--vcycle", default="mixed16", choices=["mixed16", "mixed"],
-                    help="V-cycle form of the unstructured and adjoint lines")
+    ap.add_argument("--vcycle", default="mixed", choices=["mixed16", "mixed"],
+                    help="V-cycle form of the unstructured and adjoint lines (their blocks are below 16 x 16, "
+                         "which the FP16 copy does not cover)")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":

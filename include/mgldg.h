@@ -123,7 +123,8 @@ int mgldg_ops_destroy(mgldg_ops* ops);
 #define MGLDG_PREC_MIXED         1   /* FP32 V-cycle, FP64 coarsest solve (and FP64 pcg) */
 #define MGLDG_PREC_MIXED_F16     2   /* MIXED, with the level operators' Jacobi sweeps and
                                         residuals reading a block-scaled FP16 copy (one FP32
-                                        scale per block) for square blocks 3..10 and 16 */
+                                        scale per block) where the blocks are 16 x 16; other
+                                        block sizes run as in MIXED */
 
 /* MG::Parameters (multigrid.h:48-62) plus the build's extensions. */
 typedef struct mgldg_mg_params {

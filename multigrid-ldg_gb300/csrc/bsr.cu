@@ -618,22 +618,7 @@ void bsr_ensure_fp32(mgldg_bsr* A) {
 bool spmv_f16(mgldg_ctx* ctx, const mgldg_bsr* A, float alpha, const float* x, float beta, const float* yin, float* y,
               int kclass) {
     if (!A->val16 || A->nbr == 0 || !f16_shape(A->br, A->bc)) return false;
-    switch (A->br) {
-#define MG_F16_CASE(R)                                                                                            \
-        case R:                                                                                                   \
-            launch_spmv_rows<float, R, R, __half>(ctx, A, alpha, x, beta, yin, y, nullptr, nullptr, nullptr, kclass, \
-                                                  A->val16, A->scale16);                                          \
-            return true;
-        MG_F16_CASE(3)
-        MG_F16_CASE(4)
-        MG_F16_CASE(6)
-        MG_F16_CASE(8)
-        MG_F16_CASE(9)
-        MG_F16_CASE(10)
-#undef MG_F16_CASE
-        case 16: return bulk_spmv_f16(ctx, A, alpha, x, beta, yin, y, kclass);
-    }
-    return false;
+    return bulk_spmv_f16(ctx, A, alpha, x, beta, yin, y, kclass);
 }
 
 // one thread per block: scale = largest magnitude, entries / scale in FP16

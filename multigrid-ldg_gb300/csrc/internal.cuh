@@ -209,10 +209,11 @@ bool spmv_f16(mgldg_ctx* ctx, const mgldg_bsr* A, float alpha, const float* x, f
               int kclass);
 bool jacobi_f16(mgldg_ctx* ctx, const mgldg_bsr* A, const float* Dinv, const float* b, const float* xin, float* xout,
                 float omega);
-// block sizes with FP16 kernels (square 3..10 and 16)
-inline bool f16_shape(int br, int bc) {
-    return br == bc && (br == 3 || br == 4 || br == 6 || br == 8 || br == 9 || br == 10 || br == 16);
-}
+// block sizes read from the FP16 copy: 16x16 only.  The small-block kernels
+// (3..10) are bound by load latency rather than bytes, and an FP16 copy made
+// them slower (392k-triangle disk solve 53 -> 72 ms), so those levels keep
+// FP32 in the F16 form.
+inline bool f16_shape(int br, int bc) { return br == 16 && bc == 16; }
 template <class T>
 const T* bsr_vals(const mgldg_bsr* A);
 // y = alpha*A*x + beta*yin (yin may alias y or be null when beta == 0);

@@ -12,8 +12,8 @@
 // residuals, dot products and updates in FP64.  MGLDG_PREC_MIXED_F16 is the
 // mixed form with the level operators' Jacobi sweeps and residuals reading a
 // block-scaled FP16 copy (one FP32 scale per block, entries / scale in FP16)
-// where the block shape has such kernels (square 3..10 and 16); everything
-// else, including the inverse diagonal blocks and the transfers, stays FP32.
+// where the blocks are 16 x 16 (f16_shape); everything else, including the
+// inverse diagonal blocks and the transfers, stays FP32.
 #include <algorithm>
 #include <chrono>
 #include <cmath>

@@ -483,21 +483,7 @@ void jacobi_sweep(mgldg_ctx* ctx, const mgldg_bsr* A, const T* vals, const T* Di
 bool jacobi_f16(mgldg_ctx* ctx, const mgldg_bsr* A, const float* Dinv, const float* b, const float* xin, float* xout,
                 float omega) {
     if (!A->val16 || A->blk || A->nbr == 0 || !f16_shape(A->br, A->bc)) return false;
-    switch (A->br) {
-#define MG_F16_CASE(R)                                                                                        \
-        case R:                                                                                               \
-            launch_jacobi_rows<float, R, __half>(ctx, A, A->val16, Dinv, b, xin, xout, omega, A->scale16);    \
-            return true;
-        MG_F16_CASE(3)
-        MG_F16_CASE(4)
-        MG_F16_CASE(6)
-        MG_F16_CASE(8)
-        MG_F16_CASE(9)
-        MG_F16_CASE(10)
-#undef MG_F16_CASE
-        case 16: return bulk_jacobi_f16(ctx, A, Dinv, b, xin, xout, omega);
-    }
-    return false;
+    return bulk_jacobi_f16(ctx, A, Dinv, b, xin, xout, omega);
 }
 
 template void jacobi_sweep<double>(mgldg_ctx*, const mgldg_bsr*, const double*, const double*, const double*,
