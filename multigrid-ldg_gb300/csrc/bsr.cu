@@ -621,6 +621,25 @@ bool spmv_f16(mgldg_ctx* ctx, const mgldg_bsr* A, float alpha, const float* x, f
     return bulk_spmv_f16(ctx, A, alpha, x, beta, yin, y, kclass);
 }
 
+__global__ void k_to_lo32(int64_t n, const double* __restrict__ a, float* __restrict__ lo) {
+    for (int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (int64_t)gridDim.x * 256) {
+        const double v = a[i];
+        lo[i] = (float)(v - (double)(float)v);
+    }
+}
+
+void bsr_ensure_lo32(mgldg_bsr* A) {
+    if (A->lo32) return;
+    const int64_t n = A->nvals_blocks() * (int64_t)A->bsz();
+    A->lo32 = dalloc<float>(std::max<int64_t>(1, n));
+    if (n) {
+        const int g = (int)std::min<int64_t>((n + 255) / 256, A->ctx->sm_count * 32);
+        Launch L(A->ctx, MGLDG_K_SETUP);
+        k_to_lo32<<<g, 256, 0, A->ctx->stream>>>(n, A->val, A->lo32);
+    }
+    check_launch();
+}
+
 // one thread per block: scale = largest magnitude, entries / scale in FP16
 __global__ void k_to_f16(int64_t nblk, int bsz, const double* __restrict__ a, __half* __restrict__ h,
                          float* __restrict__ scale) {
@@ -657,6 +676,7 @@ mgldg_bsr::~mgldg_bsr() {
     dfree(val32);
     dfree(val16);
     dfree(scale16);
+    dfree(lo32);
     dfree(blk);
     dfree(diag);
 }

@@ -174,6 +174,9 @@ struct mgldg_bsr {
     // spare entries (bulk copies move whole 16-byte words)
     __half* val16 = nullptr;
     float* scale16 = nullptr;
+    // low half of a two-float split of the FP64 values: val = val32 + lo32
+    // to about 2^-48 (mixed forms' double-float outer products)
+    float* lo32 = nullptr;
     int* blk = nullptr;          // optional block indirection
     std::vector<int> h_blk;
     int64_t nuniq = 0;
@@ -203,6 +206,7 @@ mgldg_bsr* bsr_new(mgldg_ctx* ctx, int nbr, int nbc, int br, int bc,
 void bsr_build_diag(mgldg_bsr* A);
 void bsr_ensure_fp32(mgldg_bsr* A);
 void bsr_ensure_f16(mgldg_bsr* A);
+void bsr_ensure_lo32(mgldg_bsr* A);
 // V-cycle products on the block-scaled FP16 copy (FP32 vectors and
 // arithmetic); false when the matrix has no such copy or the shape has no kernel
 bool spmv_f16(mgldg_ctx* ctx, const mgldg_bsr* A, float alpha, const float* x, float beta, const float* yin, float* y,

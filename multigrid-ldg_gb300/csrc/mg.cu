@@ -312,10 +312,127 @@ __global__ void __launch_bounds__(256) k_pcg_dir(int64_t n, const PcgScalars* sc
         d[i] = s[i] + beta * d[i];
 }
 
+// ------------------------------------------------- double-float outer product --
+// In the mixed forms the outer CG's q = A d runs on the FP32 pipes in
+// double-float arithmetic (GB300's FP64 rate bounds the FP64 product at about
+// 1 TFLOP/s, below HBM): A = A_hi + A_lo (val32 + lo32) and d = d_hi + d_lo
+// as float pairs, each product a*d formed as the exact FP32 product of the
+// high parts (its error recovered with an FMA) plus the two cross terms,
+// accumulated as an unnormalised (sum, error) float pair with a two-sum per
+// product (Dekker's and Knuth's error-free transformations).  Relative error
+// of a row sum about 2^-44 of sum |a d|; the lane pair's sums, the output
+// and the fused q.d are FP64.  16 x 16 blocks, one warp per block row.
+// (explicitly rounded operations: a product contracted into the two-sum's
+// addition would break the error-free identities)
+__device__ __forceinline__ void df_fma(float& sh, float& sl, float ah, float al, float dh, float dl) {
+    const float p = __fmul_rn(ah, dh);
+    const float pe = fmaf(ah, dh, -p);
+    const float t = fmaf(ah, dl, fmaf(al, dh, pe));
+    const float s = __fadd_rn(sh, p);
+    const float bb = __fsub_rn(s, sh);
+    const float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    sh = s;
+    sl = __fadd_rn(sl, __fadd_rn(e, t));
+}
+
+__global__ void __launch_bounds__(256) k_spmv_df64(int nbr, const int* __restrict__ row_ptr,
+                                                   const int* __restrict__ col_idx, const float* __restrict__ ahi,
+                                                   const float* __restrict__ alo, const float* __restrict__ dhi,
+                                                   const float* __restrict__ dlo, const double* __restrict__ d,
+                                                   double* __restrict__ q, double* __restrict__ partials) {
+    __shared__ double sm[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int r = lane >> 1, c0 = (lane & 1) * 8;
+    double dacc = 0;
+    for (int row = blockIdx.x * 8 + warp; row < nbr; row += gridDim.x * 8) {
+        const int k0 = __ldg(row_ptr + row), k1 = __ldg(row_ptr + row + 1);
+        float sh = 0.f, sl = 0.f;
+#pragma unroll 2
+        for (int k = k0; k < k1; ++k) {
+            const int j = __ldg(col_idx + k);
+            const float4* ah = reinterpret_cast<const float4*>(ahi + (size_t)k * 256 + r * 16 + c0);
+            const float4* al = reinterpret_cast<const float4*>(alo + (size_t)k * 256 + r * 16 + c0);
+            const float4* xh = reinterpret_cast<const float4*>(dhi + (size_t)j * 16 + c0);
+            const float4* xl = reinterpret_cast<const float4*>(dlo + (size_t)j * 16 + c0);
+            const float4 a0 = __ldg(ah), a1 = __ldg(ah + 1), l0 = __ldg(al), l1 = __ldg(al + 1);
+            const float4 h0 = __ldg(xh), h1 = __ldg(xh + 1), e0 = __ldg(xl), e1 = __ldg(xl + 1);
+            df_fma(sh, sl, a0.x, l0.x, h0.x, e0.x);
+            df_fma(sh, sl, a0.y, l0.y, h0.y, e0.y);
+            df_fma(sh, sl, a0.z, l0.z, h0.z, e0.z);
+            df_fma(sh, sl, a0.w, l0.w, h0.w, e0.w);
+            df_fma(sh, sl, a1.x, l1.x, h1.x, e1.x);
+            df_fma(sh, sl, a1.y, l1.y, h1.y, e1.y);
+            df_fma(sh, sl, a1.z, l1.z, h1.z, e1.z);
+            df_fma(sh, sl, a1.w, l1.w, h1.w, e1.w);
+        }
+        double v = (double)sh + (double)sl;
+        v += __shfl_xor_sync(0xffffffffu, v, 1);
+        if ((lane & 1) == 0) {
+            const size_t o = (size_t)row * 16 + r;
+            q[o] = v;
+            dacc += v * d[o];
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) dacc += __shfl_xor_sync(0xffffffffu, dacc, o);
+    if (lane == 0) sm[warp] = dacc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < 8; ++w) t += sm[w];
+        partials[blockIdx.x] = t;
+    }
+}
+
+// d as a float pair: hi = fl32(d), lo = fl32(d - hi)
+__global__ void __launch_bounds__(256) k_split(int64_t n, const double* __restrict__ d, float* __restrict__ hi,
+                                               float* __restrict__ lo) {
+    for (int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (int64_t)gridDim.x * 256) {
+        const double v = d[i];
+        const float h = (float)v;
+        hi[i] = h;
+        lo[i] = (float)(v - (double)h);
+    }
+}
+
+// d = s + beta d, and its float pair
+__global__ void __launch_bounds__(256) k_pcg_dir_split(int64_t n, const PcgScalars* sc, const double* __restrict__ s,
+                                                       double* __restrict__ d, float* __restrict__ hi,
+                                                       float* __restrict__ lo) {
+    const double beta = sc->beta;
+    for (int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (int64_t)gridDim.x * 256) {
+        const double v = s[i] + beta * d[i];
+        d[i] = v;
+        const float h = (float)v;
+        hi[i] = h;
+        lo[i] = (float)(v - (double)h);
+    }
+}
+
+static bool df64_ok(const mgldg_mg* m, const mgldg_bsr* A) {
+    return m->p.precision != MGLDG_PREC_FP64 && A->br == 16 && A->bc == 16 && !A->blk && A->val32 && A->lo32;
+}
+
+static void spmv_df64(mgldg_ctx* ctx, const mgldg_bsr* A, const mgldg_mg* m, double* partials, int* np) {
+    const int grid = std::max(1, std::min(std::min((A->nbr + 7) / 8, ctx->sm_count * 16), ctx->n_partials));
+    {
+        Launch L(ctx, MGLDG_K_SPMV);
+        k_spmv_df64<<<grid, 256, 0, ctx->stream>>>(A->nbr, A->row_ptr, A->col_idx, A->val32, A->lo32, m->dhi,
+                                                   m->dlo, m->d, m->q, partials);
+    }
+    check_launch();
+    *np = grid;
+}
+
 static void ensure_pcg(mgldg_mg* m, mgldg_ctx* ctx, int64_t n, int maxit) {
     if (m->pcg_n != n) {
-        dfree(m->r); dfree(m->d); dfree(m->q); dfree(m->s);
+        dfree(m->r); dfree(m->d); dfree(m->q); dfree(m->s); dfree(m->dhi); dfree(m->dlo);
+        m->dhi = m->dlo = nullptr;
         m->r = dalloc<double>(n); m->d = dalloc<double>(n); m->q = dalloc<double>(n); m->s = dalloc<double>(n);
+        if (m->p.precision != MGLDG_PREC_FP64) {
+            m->dhi = dalloc<float>(n);
+            m->dlo = dalloc<float>(n);
+        }
         m->pcg_n = n;
     }
     if (m->pcg_maxit < maxit) {
@@ -407,9 +524,14 @@ static void pcg_dev(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const doubl
     double* part = ctx->d_partials;
     int np = 0;
     // r = b - A x ; d = M(r) ; delta_new = delta_0 = r.d
+    const bool df = df64_ok(m, A) && m->dhi;
     spmv<double>(ctx, A, -1.0, x, 1.0, b, m->r);
     precon(m, m->r, m->d);
     dot_partials<double>(ctx, (int)n, m->r, m->d, part, &np);
+    if (df) {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_split<<<grid_vec, 256, 0, ctx->stream>>>(n, m->d, m->dhi, m->dlo);
+    }
     {
         Launch L(ctx, MGLDG_K_VECTOR);
         k_pcg_init<<<1, 256, 0, ctx->stream>>>(m->sc, part, np);
@@ -424,7 +546,8 @@ static void pcg_dev(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const doubl
     if (broke) maxit = 0;
     while (i < maxit && m->h_sc->delta_new > tol2 * m->h_sc->delta0) {
         // q = A d ; alpha = delta_new / d.q
-        spmv<double>(ctx, A, 1.0, m->d, 0.0, nullptr, m->q, m->d, part, &np);
+        if (df) spmv_df64(ctx, A, m, part, &np);
+        else spmv<double>(ctx, A, 1.0, m->d, 0.0, nullptr, m->q, m->d, part, &np);
         {
             Launch L(ctx, MGLDG_K_VECTOR);
             k_pcg_alpha<<<1, 256, 0, ctx->stream>>>(m->sc, part, np);
@@ -461,7 +584,8 @@ static void pcg_dev(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const doubl
         check_launch();
         {
             Launch L(ctx, MGLDG_K_VECTOR);
-            k_pcg_dir<<<grid_vec, 256, 0, ctx->stream>>>(n, m->sc, m->s, m->d);
+            if (df) k_pcg_dir_split<<<grid_vec, 256, 0, ctx->stream>>>(n, m->sc, m->s, m->d, m->dhi, m->dlo);
+            else k_pcg_dir<<<grid_vec, 256, 0, ctx->stream>>>(n, m->sc, m->s, m->d);
         }
         check_launch();
         MG_CHECK_CUDA(cudaMemcpyAsync(m->h_sc, m->sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost, ctx->stream));
@@ -494,7 +618,7 @@ mgldg_mg::~mgldg_mg() {
         delete L.Tt;
     }
     dfree(Cinv);
-    dfree(r); dfree(d); dfree(q); dfree(s); dfree(hist);
+    dfree(r); dfree(d); dfree(q); dfree(s); dfree(hist); dfree(dhi); dfree(dlo);
     dfree(sc);
     if (h_sc) cudaFreeHost(h_sc);
     mg::batch_free(batch);
@@ -543,6 +667,9 @@ static void level_alloc(mgldg_ctx* ctx, mgldg_mg* m, LevelData& L, bool need_sch
         bsr_ensure_fp32(const_cast<mgldg_bsr*>(L.A));
         if (m->p.precision == MGLDG_PREC_MIXED_F16 && !L.A->blk && f16_shape(L.A->br, L.A->bc))
             bsr_ensure_f16(const_cast<mgldg_bsr*>(L.A));
+        // the finest operator is the outer CG's: its double-float split
+        if (&L == &m->L[0] && L.A->br == 16 && L.A->bc == 16 && !L.A->blk)
+            bsr_ensure_lo32(const_cast<mgldg_bsr*>(L.A));
         L.Dinv32 = dalloc<float>((size_t)L.ne * L.b * L.b);
         convert<double, float>(ctx, (int64_t)L.ne * L.b * L.b, L.Dinv, L.Dinv32);
         L.x32 = dalloc<float>(L.n); L.b32 = dalloc<float>(L.n); L.r32 = dalloc<float>(L.n); L.xt32 = dalloc<float>(L.n);

@@ -66,6 +66,7 @@ struct mgldg_mg {
     int nc = 0;
     // pcg work space
     double *r = nullptr, *d = nullptr, *q = nullptr, *s = nullptr, *hist = nullptr;
+    float *dhi = nullptr, *dlo = nullptr;   // d as a float pair (mixed forms, double-float q = A d)
     int64_t pcg_n = 0;
     int pcg_maxit = 0;
     mg::PcgScalars* sc = nullptr;
