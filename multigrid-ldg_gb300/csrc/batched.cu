@@ -571,6 +571,7 @@ struct Batch {
     bool tuned = false;
     // block PCG
     double *R = nullptr, *D = nullptr, *Q = nullptr, *S = nullptr, *hist = nullptr;
+    float *Dhi = nullptr, *Dlo = nullptr;   // D as float pairs (mixed forms' double-float Q = A D)
     int64_t pcg_nk = 0;
     int hist_len = 0;
     double* partials = nullptr;
@@ -606,7 +607,7 @@ void batch_free(Batch* b) {
         dfree(L.x); dfree(L.b); dfree(L.r); dfree(L.xt);
         dfree(L.x32); dfree(L.b32); dfree(L.r32); dfree(L.xt32);
     }
-    dfree(b->R); dfree(b->D); dfree(b->Q); dfree(b->S); dfree(b->hist);
+    dfree(b->R); dfree(b->D); dfree(b->Q); dfree(b->S); dfree(b->hist); dfree(b->Dhi); dfree(b->Dlo);
     dfree(b->partials);
     dfree(b->sc_mem);
     dfree(b->sc_int);
@@ -906,6 +907,141 @@ static void bprecon(mgldg_mg* m, const double* R, double* S, bool x_is_zero) {
     }
 }
 
+// ------------------------------------------- double-float outer SpMM (mixed) --
+// Q = A D for the mixed forms on the FP32 pipes: A = val32 + lo32 and D =
+// Dhi + Dlo as float pairs, each product exact in its high part (FMA error
+// recovery) plus the cross terms, two-sum accumulation with explicitly
+// rounded operations (about 2^-44 relative), Q in FP64.  One warp per block
+// row, both halves of each block staged (transposed) in shared memory, the
+// lane owning V consecutive columns of the column tile.
+__device__ __forceinline__ void df_acc(float& sh, float& sl, float ah, float al, float dh, float dl) {
+    const float p = __fmul_rn(ah, dh);
+    const float pe = fmaf(ah, dh, -p);
+    const float t = fmaf(ah, dl, fmaf(al, dh, pe));
+    const float s = __fadd_rn(sh, p);
+    const float bb = __fsub_rn(s, sh);
+    const float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    sh = s;
+    sl = __fadd_rn(sl, __fadd_rn(e, t));
+}
+
+template <int B, int V>
+__global__ void __launch_bounds__(256) k_spmm_df64(int nbr, const int* __restrict__ row_ptr,
+                                                   const int* __restrict__ col_idx, const float* __restrict__ ahi,
+                                                   const float* __restrict__ alo, const float* __restrict__ Dhi,
+                                                   const float* __restrict__ Dlo, int k, double* __restrict__ Q) {
+    using S = Stage<B, B>;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    float* sth = reinterpret_cast<float*>(smraw) + (size_t)warp * 2 * S::SIZE;
+    float* stl = sth + S::SIZE;
+    const int c = (blockIdx.y * 32 + lane) * V;
+    const bool cok = c < k;
+    for (int i = blockIdx.x * wpb + warp; i < nbr; i += gridDim.x * wpb) {
+        float sh[B][V], sl[B][V];
+#pragma unroll
+        for (int r = 0; r < B; ++r)
+#pragma unroll
+            for (int v = 0; v < V; ++v) sh[r][v] = sl[r][v] = 0.f;
+        const int k0 = row_ptr[i], k1 = row_ptr[i + 1];
+        for (int kk = k0; kk < k1; ++kk) {
+            const int j = col_idx[kk];
+            float ph[S::PER], pl[S::PER];
+            stage_fetch<float, B, B>(ahi + (size_t)kk * (B * B), lane, ph);
+            stage_fetch<float, B, B>(alo + (size_t)kk * (B * B), lane, pl);
+            __syncwarp();
+            stage_store<float, B, B>(sth, lane, ph);
+            stage_store<float, B, B>(stl, lane, pl);
+            __syncwarp();
+            if (cok) {
+                const size_t xb = (size_t)j * B * k + c;
+#pragma unroll
+                for (int cc = 0; cc < B; ++cc) {
+                    float xh[V], xl[V];
+                    VecIO<float, V>::ld(Dhi + xb + (size_t)cc * k, xh);
+                    VecIO<float, V>::ld(Dlo + xb + (size_t)cc * k, xl);
+#pragma unroll
+                    for (int r = 0; r < B; ++r) {
+                        const float ah = sth[cc * S::BRP + r], al = stl[cc * S::BRP + r];
+#pragma unroll
+                        for (int v = 0; v < V; ++v) df_acc(sh[r][v], sl[r][v], ah, al, xh[v], xl[v]);
+                    }
+                }
+            }
+        }
+        if (cok) {
+            const size_t y0 = (size_t)i * B * k + c;
+#pragma unroll
+            for (int r = 0; r < B; ++r)
+#pragma unroll
+                for (int v = 0; v < V; ++v) Q[y0 + (size_t)r * k + v] = (double)sh[r][v] + (double)sl[r][v];
+        }
+    }
+}
+
+// float pair of D (all columns, or the active ones after a direction update)
+__global__ void __launch_bounds__(256) k_bsplit(int64_t nk, const double* __restrict__ d, float* __restrict__ hi,
+                                                float* __restrict__ lo) {
+    for (int64_t e = (int64_t)blockIdx.x * 256 + threadIdx.x; e < nk; e += (int64_t)gridDim.x * 256) {
+        const double v = d[e];
+        const float h = (float)v;
+        hi[e] = h;
+        lo[e] = (float)(v - (double)h);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_bpcg_dir_split(int64_t nk, int k, BatchScalars sc, const double* __restrict__ s,
+                                                        double* __restrict__ d, float* __restrict__ hi,
+                                                        float* __restrict__ lo) {
+    for (int64_t e = (int64_t)blockIdx.x * 256 + threadIdx.x; e < nk; e += (int64_t)gridDim.x * 256) {
+        const int c = (int)(e % k);
+        if (sc.active[c]) {
+            const double v = s[e] + sc.beta[c] * d[e];
+            d[e] = v;
+            const float h = (float)v;
+            hi[e] = h;
+            lo[e] = (float)(v - (double)h);
+        }
+    }
+}
+
+static bool df64_batch_ok(const mgldg_mg* m, const mgldg_bsr* A) {
+    const Batch* b = m->batch;
+    return m->p.precision != MGLDG_PREC_FP64 && b->Dhi && A->val32 && A->lo32 && !A->blk && A->br == A->bc &&
+           (A->br == 4 || A->br == 6 || A->br == 9 || A->br == 10 || A->br == 16);
+}
+
+template <int B>
+static void launch_spmm_df64(mgldg_ctx* ctx, const mgldg_bsr* A, const float* Dhi, const float* Dlo, int k, double* Q) {
+    constexpr int wpb = 8;
+    const bool v2 = k % 2 == 0 && k >= 64;
+    const int V = v2 ? 2 : 1;
+    const int ncolt = (k + 32 * V - 1) / (32 * V);
+    const size_t smem = (size_t)wpb * 2 * Stage<B, B>::SIZE * sizeof(float);
+    const int gx = std::max(1, std::min((A->nbr + wpb - 1) / wpb, ctx->sm_count * 16 / std::max(1, ncolt) + 1));
+    dim3 grid(gx, ncolt);
+    {
+        Launch L(ctx, MGLDG_K_SPMV);
+        if (v2) k_spmm_df64<B, 2><<<grid, wpb * 32, smem, ctx->stream>>>(A->nbr, A->row_ptr, A->col_idx, A->val32,
+                                                                          A->lo32, Dhi, Dlo, k, Q);
+        else k_spmm_df64<B, 1><<<grid, wpb * 32, smem, ctx->stream>>>(A->nbr, A->row_ptr, A->col_idx, A->val32,
+                                                                       A->lo32, Dhi, Dlo, k, Q);
+    }
+    check_launch();
+}
+
+static void outer_spmm_df64(mgldg_mg* m, const mgldg_bsr* A, double* Q) {
+    const Batch* b = m->batch;
+    switch (A->br) {
+        case 4: launch_spmm_df64<4>(m->ctx, A, b->Dhi, b->Dlo, b->k, Q); return;
+        case 6: launch_spmm_df64<6>(m->ctx, A, b->Dhi, b->Dlo, b->k, Q); return;
+        case 9: launch_spmm_df64<9>(m->ctx, A, b->Dhi, b->Dlo, b->k, Q); return;
+        case 10: launch_spmm_df64<10>(m->ctx, A, b->Dhi, b->Dlo, b->k, Q); return;
+        case 16: launch_spmm_df64<16>(m->ctx, A, b->Dhi, b->Dlo, b->k, Q); return;
+    }
+    throw Error(MGLDG_ERR_UNSUPPORTED, "double-float SpMM: unsupported block size");
+}
+
 static void outer_spmm(mgldg_mg* m, const mgldg_bsr* A, double alpha, const double* X, double beta, const double* Yin,
                        double* Y) {
     SpmmArgs<double> a = args_of<double>(A, bsr_vals<double>(A), m->batch->k);
@@ -920,9 +1056,13 @@ static void outer_spmm(mgldg_mg* m, const mgldg_bsr* A, double alpha, const doub
 static void ensure_bpcg(mgldg_mg* m, int64_t nk, int maxit) {
     Batch* b = m->batch;
     if (b->pcg_nk != nk) {
-        dfree(b->R); dfree(b->D); dfree(b->Q); dfree(b->S);
-        b->R = nullptr; b->D = nullptr; b->Q = nullptr; b->S = nullptr;
+        dfree(b->R); dfree(b->D); dfree(b->Q); dfree(b->S); dfree(b->Dhi); dfree(b->Dlo);
+        b->R = nullptr; b->D = nullptr; b->Q = nullptr; b->S = nullptr; b->Dhi = nullptr; b->Dlo = nullptr;
         b->R = dalloc<double>(nk); b->D = dalloc<double>(nk); b->Q = dalloc<double>(nk); b->S = dalloc<double>(nk);
+        if (m->p.precision != MGLDG_PREC_FP64) {
+            b->Dhi = dalloc<float>(nk);
+            b->Dlo = dalloc<float>(nk);
+        }
         b->pcg_nk = nk;
     }
     const int len = std::max(1, maxit) * b->k;
@@ -950,9 +1090,14 @@ static void bpcg(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, int k, const d
     const double tol2 = tol * tol;
     int np = 0;
     // R = B - A X ; D = M(R) ; delta = colsum(R o D)
+    const bool df = df64_batch_ok(m, A);
     outer_spmm(m, A, -1.0, X, 1.0, B, b->R);
     bprecon(m, b->R, b->D, true);
     coldot<double>(ctx, n, k, b->R, b->D, b->partials, &np);
+    if (df) {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_bsplit<<<gvec, 256, 0, ctx->stream>>>(nk, b->D, b->Dhi, b->Dlo);
+    }
     {
         Launch L(ctx, MGLDG_K_VECTOR);
         k_bpcg_init<<<gk, 128, 0, ctx->stream>>>(k, sc, b->partials, np, tol2, maxit);
@@ -968,7 +1113,8 @@ static void bpcg(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, int k, const d
     int i = 0;
     while (b->h_counter[0] > 0) {
         // Q = A D ; alpha = delta / colsum(D o Q)
-        outer_spmm(m, A, 1.0, b->D, 0.0, nullptr, b->Q);
+        if (df) outer_spmm_df64(m, A, b->Q);
+        else outer_spmm(m, A, 1.0, b->D, 0.0, nullptr, b->Q);
         coldot<double>(ctx, n, k, b->D, b->Q, b->partials, &np);
         {
             Launch L(ctx, MGLDG_K_VECTOR);
@@ -998,7 +1144,8 @@ static void bpcg(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, int k, const d
         check_launch();
         {
             Launch L(ctx, MGLDG_K_VECTOR);
-            k_bpcg_dir<<<gvec, 256, 0, ctx->stream>>>(nk, k, sc, b->S, b->D);
+            if (df) k_bpcg_dir_split<<<gvec, 256, 0, ctx->stream>>>(nk, k, sc, b->S, b->D, b->Dhi, b->Dlo);
+            else k_bpcg_dir<<<gvec, 256, 0, ctx->stream>>>(nk, k, sc, b->S, b->D);
         }
         {
             Launch L(ctx, MGLDG_K_VECTOR);

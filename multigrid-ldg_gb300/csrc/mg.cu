@@ -668,8 +668,9 @@ static void level_alloc(mgldg_ctx* ctx, mgldg_mg* m, LevelData& L, bool need_sch
         if (m->p.precision == MGLDG_PREC_MIXED_F16 && !L.A->blk && f16_shape(L.A->br, L.A->bc))
             bsr_ensure_f16(const_cast<mgldg_bsr*>(L.A));
         // the finest operator is the outer CG's: its double-float split
-        if (&L == &m->L[0] && L.A->br == 16 && L.A->bc == 16 && !L.A->blk)
-            bsr_ensure_lo32(const_cast<mgldg_bsr*>(L.A));
+        // (single-RHS products use it for 16 x 16 blocks, multi-RHS ones for
+        // square blocks 4..16)
+        if (&L == &m->L[0] && !L.A->blk) bsr_ensure_lo32(const_cast<mgldg_bsr*>(L.A));
         L.Dinv32 = dalloc<float>((size_t)L.ne * L.b * L.b);
         convert<double, float>(ctx, (int64_t)L.ne * L.b * L.b, L.Dinv, L.Dinv32);
         L.x32 = dalloc<float>(L.n); L.b32 = dalloc<float>(L.n); L.r32 = dalloc<float>(L.n); L.xt32 = dalloc<float>(L.n);
