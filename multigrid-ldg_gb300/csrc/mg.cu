@@ -24,6 +24,7 @@
 
 #include "api.cuh"
 #include "mg.cuh"
+#include "rowdot.cuh"
 
 using namespace mg;
 
@@ -384,6 +385,64 @@ __global__ void __launch_bounds__(256) k_spmv_df64(int nbr, const int* __restric
     }
 }
 
+// The same product for square blocks of 3..10 (triangles, tetrahedra,
+// agglomerated levels): 32 / B block rows per warp, lane (g, c) owning block
+// column c as in the small-block kernels (coalesced rows of each block, one
+// entry of each d pair), B double-float partial sums per lane, reduced in
+// FP64 through shared memory in column order.
+template <int B>
+__global__ void __launch_bounds__(256) k_spmv_rows_df64(int nbr, const int* __restrict__ row_ptr,
+                                                        const int* __restrict__ col_idx, const float* __restrict__ ahi,
+                                                        const float* __restrict__ alo, const float* __restrict__ dhi,
+                                                        const float* __restrict__ dlo, const double* __restrict__ d,
+                                                        double* __restrict__ q, double* __restrict__ partials) {
+    using R = Rows<B>;
+    __shared__ double sr[8 * R::SM];
+    __shared__ double sm[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane / R::S, c = lane - g * R::S;
+    double* sw = sr + warp * R::SM;
+    double dacc = 0;
+    const int nw = gridDim.x * 8;
+    for (int base = (blockIdx.x * 8 + warp) * R::G; base < nbr; base += nw * R::G) {
+        const int row = base + g;
+        const bool valid = g < R::G && row < nbr;
+        float sh[B], sl[B];
+#pragma unroll
+        for (int r = 0; r < B; ++r) sh[r] = sl[r] = 0.f;
+        if (valid) {
+            const int k0 = __ldg(row_ptr + row), k1 = __ldg(row_ptr + row + 1);
+#pragma unroll 2
+            for (int k = k0; k < k1; ++k) {
+                const int j = __ldg(col_idx + k);
+                const float xh = __ldg(dhi + (size_t)j * B + c), xl = __ldg(dlo + (size_t)j * B + c);
+                const float* ph = ahi + (size_t)k * (B * B) + c;
+                const float* pl = alo + (size_t)k * (B * B) + c;
+#pragma unroll
+                for (int r = 0; r < B; ++r) df_fma(sh[r], sl[r], __ldg(ph + r * B), __ldg(pl + r * B), xh, xl);
+            }
+        }
+        double acc[B];
+#pragma unroll
+        for (int r = 0; r < B; ++r) acc[r] = (double)sh[r] + (double)sl[r];
+        const double v = rows_reduce<double, B, B>(acc, sw, g, c, g < R::G);
+        if (valid) {
+            const size_t o = (size_t)row * B + c;
+            q[o] = v;
+            dacc += v * d[o];
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) dacc += __shfl_xor_sync(0xffffffffu, dacc, o);
+    if (lane == 0) sm[warp] = dacc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < 8; ++w) t += sm[w];
+        partials[blockIdx.x] = t;
+    }
+}
+
 // d as a float pair: hi = fl32(d), lo = fl32(d - hi)
 __global__ void __launch_bounds__(256) k_split(int64_t n, const double* __restrict__ d, float* __restrict__ hi,
                                                float* __restrict__ lo) {
@@ -409,19 +468,45 @@ __global__ void __launch_bounds__(256) k_pcg_dir_split(int64_t n, const PcgScala
     }
 }
 
+static bool df64_shape(int b) { return b == 3 || b == 4 || b == 6 || b == 8 || b == 9 || b == 10 || b == 16; }
+
 static bool df64_ok(const mgldg_mg* m, const mgldg_bsr* A) {
-    return m->p.precision != MGLDG_PREC_FP64 && A->br == 16 && A->bc == 16 && !A->blk && A->val32 && A->lo32;
+    return m->p.precision != MGLDG_PREC_FP64 && A->br == A->bc && df64_shape(A->br) && !A->blk && A->val32 &&
+           A->lo32;
+}
+
+template <int B>
+static int launch_rows_df64(mgldg_ctx* ctx, const mgldg_bsr* A, const mgldg_mg* m, double* partials) {
+    const int rows_per_cta = 8 * Rows<B>::G;
+    const int grid =
+        std::max(1, std::min(std::min((A->nbr + rows_per_cta - 1) / rows_per_cta, ctx->sm_count * 8), ctx->n_partials));
+    Launch L(ctx, MGLDG_K_SPMV);
+    k_spmv_rows_df64<B><<<grid, 256, 0, ctx->stream>>>(A->nbr, A->row_ptr, A->col_idx, A->val32, A->lo32, m->dhi,
+                                                       m->dlo, m->d, m->q, partials);
+    return grid;
 }
 
 static void spmv_df64(mgldg_ctx* ctx, const mgldg_bsr* A, const mgldg_mg* m, double* partials, int* np) {
-    const int grid = std::max(1, std::min(std::min((A->nbr + 7) / 8, ctx->sm_count * 16), ctx->n_partials));
-    {
-        Launch L(ctx, MGLDG_K_SPMV);
-        k_spmv_df64<<<grid, 256, 0, ctx->stream>>>(A->nbr, A->row_ptr, A->col_idx, A->val32, A->lo32, m->dhi,
-                                                   m->dlo, m->d, m->q, partials);
+    if (A->br == 16) {
+        const int grid = std::max(1, std::min(std::min((A->nbr + 7) / 8, ctx->sm_count * 16), ctx->n_partials));
+        {
+            Launch L(ctx, MGLDG_K_SPMV);
+            k_spmv_df64<<<grid, 256, 0, ctx->stream>>>(A->nbr, A->row_ptr, A->col_idx, A->val32, A->lo32, m->dhi,
+                                                       m->dlo, m->d, m->q, partials);
+        }
+        *np = grid;
+    } else {
+        switch (A->br) {
+            case 3: *np = launch_rows_df64<3>(ctx, A, m, partials); break;
+            case 4: *np = launch_rows_df64<4>(ctx, A, m, partials); break;
+            case 6: *np = launch_rows_df64<6>(ctx, A, m, partials); break;
+            case 8: *np = launch_rows_df64<8>(ctx, A, m, partials); break;
+            case 9: *np = launch_rows_df64<9>(ctx, A, m, partials); break;
+            case 10: *np = launch_rows_df64<10>(ctx, A, m, partials); break;
+            default: throw Error(MGLDG_ERR_UNSUPPORTED, "double-float product: unsupported block size");
+        }
     }
     check_launch();
-    *np = grid;
 }
 
 static void ensure_pcg(mgldg_mg* m, mgldg_ctx* ctx, int64_t n, int maxit) {
