@@ -5,7 +5,7 @@ Workload: the 512 x 512 uniform quadtree on [0,1]^2 with tensor-product Q3
 LDG (16 DOF per element, 4,194,304 DOF), tau0 = tauD = 1/h = 512,
 homogeneous Dirichlet data and a seeded 8-Gaussian forcing (seed 2001);
 RATRAT Galerkin hierarchy 512 -> 4 (8 levels) with a dense coarsest
-Cholesky; MG-PCG with one V(2,2) cycle as preconditioner, stopped at
+inverse; MG-PCG with one V(2,2) cycle as preconditioner, stopped at
 r.z <= (1e-10)^2 r0.z0 as the reference's pcg does.  The coarsest level is
 solved without the reference's mean projection (b -= mean(b),
 multigrid.h:367): with Dirichlet data the coarse matrix is non-singular and
@@ -45,7 +45,7 @@ WL = dict(P=4, n=512, levels=8, npre=2, npost=2, tol=1e-10, seed=2001, maxit=200
 def workload_name(n, P, levels):
     return (f"{n}x{n} uniform quadtree, Q{P - 1} LDG ({P * P} DOF/element, {n * n * P * P:,} DOF), "
             f"tau0=tauD={n}, RATRAT hierarchy {n}->{n >> (levels - 1)} ({levels} levels, dense coarsest "
-            f"Cholesky), MG-PCG V(2,2), tol 1e-10")
+            f"inverse), MG-PCG V(2,2), tol 1e-10")
 
 
 def peaks():

@@ -116,7 +116,8 @@ int mgldg_ops_destroy(mgldg_ops* ops);
 #define MGLDG_RELAX_GAUSS_SEIDEL 1   /* MG::kGaussSeidel */
 #define MGLDG_COARSE_CHOLESKY    0   /* MG::kCholesky: one-element coarsest level */
 #define MGLDG_COARSE_RELAXATION  1   /* MG::kRelaxation */
-#define MGLDG_COARSE_DENSE       2   /* extension: dense Cholesky of a multi-element coarsest level */
+#define MGLDG_COARSE_DENSE       2   /* extension: dense FP64 inverse (Gauss-Jordan) of a
+                                        multi-element coarsest level, applied as a matvec */
 #define MGLDG_RESTRICT_RAT       0   /* MG::kRAT */
 #define MGLDG_RESTRICT_RATRAT    1   /* MG::kRATRAT */
 #define MGLDG_PREC_FP64          0   /* plain form: FP64 throughout */
