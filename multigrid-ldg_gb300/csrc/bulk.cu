@@ -37,10 +37,11 @@ struct Stage {
     static constexpr int kCol = kDinv + kRows * kBlk * 4;
     static constexpr int kScl = kCol + kColInts * 4;
     static constexpr int kBytes = kScl + (sizeof(VT) == 2 ? kColInts * 4 : 0);
-    // stages per CTA: the FP16 stage holds half the bytes, so a third stage
-    // keeps about as many bytes in flight (two CTAs per SM either way)
-    static constexpr int kNS = sizeof(VT) == 2 ? 3 : 2;
-    static constexpr size_t kSmem = (size_t)kNS * kBytes;   // ~96 KiB (FP32), ~85 KiB (FP16)
+    // stages per CTA (FP16: three CTAs per SM hold about as many bytes in
+    // flight as two FP32 CTAs)
+    static constexpr int kNS = 2;
+    static constexpr size_t kSmem = (size_t)kNS * kBytes;   // ~96 KiB (FP32), ~57 KiB (FP16)
+    static constexpr int kMinBlocks = sizeof(VT) == 2 ? 3 : 2;   // CTAs per SM
     static_assert(kBytes % 16 == 0 && kCol % 16 == 0 && kScl % 16 == 0, "stage regions must stay 16-byte aligned");
 };
 }  // namespace
@@ -113,16 +114,18 @@ __device__ __forceinline__ float row_from(const float* a, const float* /*scl*/, 
 }
 
 // The same on block-scaled FP16 values: eight halves (16 bytes) per lane and
-// block, the block's partial product times its scale.
+// block, the block's partial product times its scale; three blocks in flight
+// (fewer registers, three CTAs per SM instead of two).
+constexpr int kDepth16 = 3;
 __device__ __forceinline__ float row_from(const __half* a, const float* scl, const int* cols,
                                           const float* __restrict__ x, int nb, int r, int c0, int lane) {
     float acc = 0.f;
-    for (int qb = 0; qb < nb; qb += 5) {
-        const int m = min(5, nb - qb);
+    for (int qb = 0; qb < nb; qb += kDepth16) {
+        const int m = min(kDepth16, nb - qb);
         const int jl = (lane < m) ? cols[qb + lane] : 0;
-        float4 xv[5][2];
+        float4 xv[kDepth16][2];
 #pragma unroll
-        for (int q = 0; q < 5; ++q) {
+        for (int q = 0; q < kDepth16; ++q) {
             const int j = __shfl_sync(0xffffffffu, jl, q);
             if (q < m) {
                 const float4* xp = reinterpret_cast<const float4*>(x + (size_t)j * kB + c0);
@@ -131,7 +134,7 @@ __device__ __forceinline__ float row_from(const __half* a, const float* scl, con
             }
         }
 #pragma unroll
-        for (int q = 0; q < 5; ++q)
+        for (int q = 0; q < kDepth16; ++q)
             if (q < m) {
                 const uint4 raw = *reinterpret_cast<const uint4*>(a + (size_t)(qb + q) * kBlk + r * kB + c0);
                 const __half2* h = reinterpret_cast<const __half2*>(&raw);
@@ -154,7 +157,7 @@ __device__ __forceinline__ float row_from(const __half* a, const float* scl, con
 // JACOBI: xout_i = xin_i + omega * Dinv_i (b_i - (A xin)_i)
 // else:   y_i = alpha (A x)_i + beta yin_i
 template <bool JACOBI, class VT>
-__global__ void __launch_bounds__(kRows * 32, 2)
+__global__ void __launch_bounds__(kRows * 32, Stage<VT>::kMinBlocks)
     k_rows_bulk(int nbr, const int* __restrict__ row_ptr, const int* __restrict__ col_idx, const VT* __restrict__ val,
                 const float* __restrict__ scale, const float* __restrict__ Dinv, const float* __restrict__ x,
                 const float* bvec, float* y, float alpha, float beta, float omega, unsigned* err, int64_t timeout_ns) {
@@ -316,7 +319,7 @@ static void launch_bulk(mgldg_ctx* ctx, const mgldg_bsr* A, const VT* vals, cons
         attr_set[ctx->device] = true;
     }
     const int ngroups = (A->nbr + kRows - 1) / kRows;
-    const int grid = std::max(1, std::min(ngroups, 2 * ctx->sm_count));
+    const int grid = std::max(1, std::min(ngroups, Stage<VT>::kMinBlocks * ctx->sm_count));
     {
         Launch L(ctx, kclass);
         k_rows_bulk<JACOBI, VT><<<grid, kRows * 32, Stage<VT>::kSmem, ctx->stream>>>(
