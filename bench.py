@@ -732,10 +732,10 @@ def run_gpu(args, ws, rank, local):
             roof["traffic"] = bytes0 * (418.508032 / 415.756292)
             roof["traffic_source"] = "ncu at 256x256 Q3, scaled by block rows"
         if headline == "mixed16_jacobi" and key == "jacobi":
-            # the same for the FP16-copy kernel: 253.668352 MB of DRAM
+            # the same for the FP16-copy kernel: 254.26816 MB of DRAM
             # traffic for 249.815044 MB of algorithmic bytes at 256x256 Q3
             # (profiles/k_rows_bulk_jacobi_f16_256x256_q3.md)
-            roof["traffic"] = bytes0 * (253.668352 / 249.815044)
+            roof["traffic"] = bytes0 * (254.26816 / 249.815044)
             roof["traffic_source"] = "ncu at 256x256 Q3, scaled by block rows"
     gpu_launches = int(sum(v[0] for v in prof.values()))
     results[headline]["per_level_ms"] = {k: {str(l): round(v[1] / args.steps, 4) for l, v in d.items()}
