@@ -760,9 +760,16 @@ def run_gpu(args, ws, rank, local):
 
     batched = None
     del mgs
+    import gc
+    gc.collect()
+    # the unstructured lines run before the multi-RHS line: after the 64-RHS
+    # batch (several GB of work space) the uneven batch of disks measured
+    # 128-188 ms instead of 105 ms, for reasons not determined
+    unstructured = run_unstructured(args, ctx, ext, torch, local, ws) if args.disk_h > 0 else None
+    gc.collect()
     if args.batched > 0:
         batched = run_batched(args, ctx, ext, torch, local, ws)
-    unstructured = run_unstructured(args, ctx, ext, torch, local, ws) if args.disk_h > 0 else None
+    gc.collect()
     adjoint = run_adjoint(args, ctx, ext, torch, local, ws) if args.ball_h > 0 else None
 
     speedup = {}
