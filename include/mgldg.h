@@ -121,7 +121,10 @@ int mgldg_ops_destroy(mgldg_ops* ops);
 #define MGLDG_RESTRICT_RAT       0   /* MG::kRAT */
 #define MGLDG_RESTRICT_RATRAT    1   /* MG::kRATRAT */
 #define MGLDG_PREC_FP64          0   /* plain form: FP64 throughout */
-#define MGLDG_PREC_MIXED         1   /* FP32 V-cycle, FP64 coarsest solve (and FP64 pcg) */
+#define MGLDG_PREC_MIXED         1   /* FP32 V-cycle, FP64 coarsest solve and FP64 pcg
+                                        vectors and scalars; pcg's q = A d (square blocks
+                                        3..10 and 16) in double-float arithmetic on the
+                                        FP32 pipes, about 2^-44 relative */
 #define MGLDG_PREC_MIXED_F16     2   /* MIXED, with the level operators' Jacobi sweeps and
                                         residuals reading a block-scaled FP16 copy (one FP32
                                         scale per block) where the blocks are 16 x 16; other

@@ -9,7 +9,8 @@
 // keeps FP32 copies of every level operator, inverse diagonal block and
 // transfer, runs the whole V-cycle in FP32 with FP32 accumulation, and keeps
 // the coarsest solve (mean projection and dense inverse), the outer CG
-// residuals, dot products and updates in FP64.  MGLDG_PREC_MIXED_F16 is the
+// residuals, dot products and updates in FP64 (the CG's q = A d in
+// double-float arithmetic, k_spmv_df64 below).  MGLDG_PREC_MIXED_F16 is the
 // mixed form with the level operators' Jacobi sweeps and residuals reading a
 // block-scaled FP16 copy (one FP32 scale per block, entries / scale in FP16)
 // where the blocks are 16 x 16 (f16_shape); everything else, including the
