@@ -233,3 +233,21 @@ def test_tetrahedral_coarse_bases_drop_dependent_directions():
         assert len(hist) < its, (relax, len(hist))
         A = R.to_scipy(pr.op(O.OP_A))
         assert np.linalg.norm(b - A @ x) <= 1e-9 * np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("h", [0.3, 0.1, 0.05, 0.03])
+def test_ball_mesh_quality_does_not_degrade_with_h(h):
+    # no tetrahedron has four vertices on the sphere, so no sliver flattens
+    # as h shrinks: aspect ratio (longest edge^3 / (6 sqrt2 volume), 1 for a
+    # regular tetrahedron) stays bounded
+    _lib_or_skip()
+    p, t = mgldg.ball_mesh(h)
+    on_sphere = np.abs(np.linalg.norm(p, axis=1) - 1) < 1e-12
+    assert not np.any(on_sphere[t].all(axis=1))
+    a, b, c = (p[t[:, k]] - p[t[:, 0]] for k in (1, 2, 3))
+    vol = np.einsum("ij,ij->i", a, np.cross(b, c)) / 6
+    E = np.stack([np.linalg.norm(p[t[:, i]] - p[t[:, j]], axis=1) for i in range(4) for j in range(i + 1, 4)], 1)
+    q = E.max(1) ** 3 / (6 * np.sqrt(2) * vol)
+    assert q.max() < 15 and np.median(q) < 6, (q.max(), np.median(q))
+    # Morton order already: reordering is the identity
+    assert np.array_equal(mgldg.morton_order(p, t), t)
