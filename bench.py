@@ -13,13 +13,19 @@ the projection only perturbs the correction (PCG then stalls, iteration
 counts grow with n); the parity tests keep the projection on.
 
 One step = one MG-PCG solve from x = 0 with b already in HBM.  The headline
-value is the mixed form (FP32 V-cycle, FP64 CG and coarsest solve) with
-damped block Jacobi (omega = 0.7), the fastest form; the plain FP64 form and
-the block Gauss-Seidel (omega = 0.8) variants are timed beside it.  The operator (2.68 GB in FP64)
-is larger than L2, so no flush is needed between steps.
+value is the mixed form of the workload -- FP32 BSR blocks, FP32 V-cycle,
+FP64 outer CG and coarsest solve -- with damped block Jacobi (omega = 0.7);
+the plain FP64 form, block Gauss-Seidel (omega = 0.8, the reference's exact
+sweep order) in both precisions and the FP16-stored copy of the level
+operators are timed beside it ("forms").  The operator (2.68 GB in FP64) is
+larger than L2, so no flush is needed between steps.
 
---impl reference times the CPU oracle (the restatement of the reference's
-serial solver) on a bounded sample of the same workload.
+CPU baseline: the oracle (the restatement of the reference's serial solver)
+runs the whole FP64 solve of the same problem with the same smoother on one
+host core -- setup ("Build multigrid hierarchy") and solve ("Solve using
+MGPCG") timed separately, as the reference's driver does -- in a child
+process beside the GPU measurement.  --impl reference prints that
+measurement as the reference arm.
 Multi-GPU: the path does not shard (exact Gauss-Seidel is sequential), so
 --gpus N runs N independent replicas, one per rank.
 """
@@ -133,29 +139,58 @@ def dist_barrier(ws):
 
 
 # ------------------------------------------------------------ CPU oracle --
-def cpu_baseline(n, P, levels, iters, tol, seed):
-    """Times the CPU oracle (serial restatement of the reference) on the same
-    problem: setup untimed, then one pcg call with maxit=1 (initial residual,
-    two V-cycles, one iteration); scaled to a full solve of `iters`
-    iterations as (iters + 1) / 2 of that sample."""
+REF_SMOOTHERS = {"jacobi": (0, 0.7), "gs": (1, 0.8)}   # oracle RELAX_* value, omega
+
+
+def cpu_oracle_solve(n, P, levels, smoother, tol, seed):
+    """The CPU oracle (serial restatement of the reference's solver) on the
+    full problem, timed as the reference's driver times it
+    (tests/cartesian/dg_tests.cpp:294-308): "Build multigrid hierarchy" --
+    the LDG operators and the Galerkin hierarchy -- then "Solve using MGPCG",
+    the whole pcg to the tolerance from x = 0.  FP64, one thread (the
+    reference is serial)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py as O
+    relax, omega = REF_SMOOTHERS[smoother]
     t0 = time.perf_counter()
     pr = O.Problem(P, 1.0 / n, tau0=n, tauD=n, seed=seed)
-    omg = O.Multigrid(pr, relaxation=O.RELAX_GS, omega=0.8, npre=2, npost=2, solver=O.COARSE_DENSE,
+    omg = O.Multigrid(pr, relaxation=relax, omega=omega, npre=2, npost=2, solver=O.COARSE_DENSE,
                       nlevels=levels, mean_project=False)
-    t_setup = time.perf_counter() - t0
+    setup_s = time.perf_counter() - t0
     b = pr.rhs()
     t1 = time.perf_counter()
-    pr.pcg(b, mg=omg, tol=tol, maxit=1)
-    t_sample = time.perf_counter() - t1
-    est_ms = t_sample * (iters + 1) / 2 * 1e3
-    return {"value": est_ms, "unit": "ms", "cores": 1, "kind": "port",
-            "sample": (f"oracle (serial C++ restatement of the reference, FP64 Gauss-Seidel V(2,2)) on the "
-                       f"full {n}x{n} Q{P - 1} problem: one pcg call with maxit=1 (initial residual + 2 V-cycles) "
-                       f"took {t_sample:.2f} s; scaled by ({iters}+1)/2 to the GPU FP64 iteration count; "
-                       f"oracle setup {t_setup:.1f} s not included"),
-            "sample_s": t_sample, "setup_s": t_setup}
+    _, hist, _ = pr.pcg(b, mg=omg, tol=tol, maxit=WL["maxit"])
+    solve_s = time.perf_counter() - t1
+    return {"smoother": smoother, "setup_s": setup_s, "solve_ms": solve_s * 1e3, "iters": int(len(hist))}
+
+
+def cpu_baseline_line(results, n, P):
+    """cpu_baseline object from measured full oracle solves."""
+    main = results[0]
+    text = "; ".join(f"{r['smoother']}: setup {r['setup_s']:.1f} s, solve {r['solve_ms'] / 1e3:.1f} s, "
+                     f"{r['iters']} iterations" for r in results)
+    return {"value": main["solve_ms"], "unit": "ms", "cores": 1, "kind": "port",
+            "sample": (f"the whole FP64 MG-PCG solve to 1e-10 of the oracle (serial C++ restatement of the "
+                       f"reference) on the full {n}x{n} Q{P - 1} problem, measured, not extrapolated ({text}); "
+                       f"value = the {main['smoother']} solve"),
+            "runs": results}
+
+
+def start_cpu_baseline(args):
+    """Starts the oracle's full solve in a child process (spawned before any
+    GPU work, so that it runs beside the GPU measurement on another host
+    core); returns the process, whose stdout is one JSON line."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--cpu-oracle", args.cpu_smoothers, "--n", str(args.n),
+           "--levels", str(args.levels)]
+    return subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+
+
+def finish_cpu_baseline(proc):
+    out, _ = proc.communicate()
+    for line in out.splitlines():
+        if line.startswith("["):
+            return json.loads(line)
+    return None
 
 
 # ------------------------------------------------------------- GPU forms --
@@ -180,22 +215,21 @@ def level_bytes(mg, nlev, s, f16=False):
 
 FORMS = {
     # name: (relaxation, omega, precision) -- MGLDG_RELAX_* / MGLDG_PREC_* values
-    "mixed16_jacobi": (0, 0.7, 2),
     "mixed_jacobi": (0, 0.7, 1),
     "fp64_jacobi": (0, 0.7, 0),
     "mixed_gs": (1, 0.8, 1),
     "fp64_gs": (1, 0.8, 0),
+    "mixed16_jacobi": (0, 0.7, 2),
 }
 FORM_TEXT = {"mixed16_jacobi": ("mixed precision with the level operators stored as block-scaled FP16 (one FP32 "
                                "scale per block), damped block Jacobi omega=0.7"),
-             "mixed_jacobi": "mixed precision, damped block Jacobi omega=0.7",
+             "mixed_jacobi": "mixed precision (FP32 BSR blocks, FP32 V-cycle, FP64 CG), damped block Jacobi omega=0.7",
              "fp64_jacobi": "FP64, damped block Jacobi omega=0.7",
-             "mixed_gs": "mixed precision, block Gauss-Seidel omega=0.8",
+             "mixed_gs": "mixed precision (FP32 BSR blocks, FP32 V-cycle, FP64 CG), block Gauss-Seidel omega=0.8",
              "fp64_gs": "FP64, block Gauss-Seidel omega=0.8"}
-# FP64 Gauss-Seidel MG-PCG iterations of the default workload (measured on
-# the GPU; the oracle runs the same algorithm) -- used by the reference arm,
-# which only samples the first iteration
-REF_ITERS = 16
+SMOOTHER_TEXT = {0: "damped block Jacobi omega=0.7, V(2,2)", 1: "block Gauss-Seidel omega=0.8 (exact order), V(2,2)"}
+DTYPE = {0: "f64", 1: "f32 V-cycle (FP32 BSR blocks) / f64 CG", 2: "f16-stored level operators, f32 V-cycle / f64 CG"}
+L2_TEXT = "inputs larger than L2 (A is 2.68 GB in FP64, 1.34 GB in FP32), no flush"
 
 
 def fp64_peak_tflops(torch):
@@ -703,40 +737,45 @@ def run_gpu(args, ws, rank, local):
     hbm, peak_kind = peaks()
     fp64_tf = fp64_peak_tflops(torch)
 
-    # roofline of the dominant kernel class of the headline form
-    # The dominant kernel class of the headline form, taken on the finest level
-    # (its launches carry the bytes; coarse-level launches are a few us each
-    # and their event times include launch gaps).  Algorithmic bytes per
-    # launch come from the level's actual matrix; time from CUDA events on the
-    # library's stream in the profiled pass of the same steps.
-    relax_h, _, prec_h = FORMS[headline]
-    prof, per_level = profs[headline]
-    s = 4 if prec_h in (1, 2) else 8
-    lb = level_bytes(mgs[headline], levels - 1, s, f16=prec_h == 2)
-    cls = max(prof, key=lambda k: prof[k][1])
-    key = {"gauss_seidel": "gs", "jacobi": "jacobi", "spmv": "spmv"}.get(cls)
-    roof = {"bound": "hbm", "kernel": cls, "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None,
-            "traffic": None, "peak_kind": peak_kind}
-    if key and 0 in per_level.get(cls, {}):
-        n0, ms0 = per_level[cls][0]
+    # Roofline of the dominant kernel class of the headline form, taken on the
+    # finest level (its launches carry the bytes; coarse-level launches are a
+    # few us each and their event times include launch gaps).  Algorithmic
+    # bytes per launch come from the level's actual matrix; time from CUDA
+    # events on the library's stream in the profiled pass of the same steps.
+    # traffic: dram__bytes_read.sum + dram__bytes_write.sum of the same kernel
+    # from one ncu capture at 256x256 Q3 (DRAM bytes / algorithmic bytes, the
+    # ratio below), scaled to this launch by its algorithmic bytes.
+    NCU_TRAFFIC_RATIO = {("mixed_jacobi", "jacobi"): 418.508032 / 415.756292,
+                         ("mixed16_jacobi", "jacobi"): 254.26816 / 249.815044}
+
+    def kernel_roof(form, cls, key):
+        _, _, prec = FORMS[form]
+        prof_f, per_level_f = profs[form]
+        if not key or 0 not in per_level_f.get(cls, {}):
+            return None
+        lb = level_bytes(mgs[form], levels - 1, 4 if prec in (1, 2) else 8, f16=prec == 2)
+        n0, ms0 = per_level_f[cls][0]
         bytes0 = lb[0][key]
         achieved = bytes0 * n0 / (ms0 * 1e-3) / 1e9
-        roof.update(achieved=achieved, frac=achieved / hbm, level=0, launches=n0, avg_launch_ms=ms0 / n0,
-                    algorithmic_bytes_per_launch=bytes0,
-                    all_levels={"launches": prof[cls][0], "ms": prof[cls][1]})
-        if headline == "mixed_jacobi" and key == "jacobi":
-            # dram__bytes_read.sum + dram__bytes_write.sum of this kernel
-            # from one ncu capture at 256x256 Q3 (418.5 MB for 415.8 MB of
-            # algorithmic bytes; profiles/k_rows_bulk_jacobi_fp32_256x256_q3.md),
-            # scaled to this launch by its algorithmic bytes
-            roof["traffic"] = bytes0 * (418.508032 / 415.756292)
-            roof["traffic_source"] = "ncu at 256x256 Q3, scaled by block rows"
-        if headline == "mixed16_jacobi" and key == "jacobi":
-            # the same for the FP16-copy kernel: 254.26816 MB of DRAM
-            # traffic for 249.815044 MB of algorithmic bytes at 256x256 Q3
-            # (profiles/k_rows_bulk_jacobi_f16_256x256_q3.md)
-            roof["traffic"] = bytes0 * (254.26816 / 249.815044)
-            roof["traffic_source"] = "ncu at 256x256 Q3, scaled by block rows"
+        r = {"bound": "hbm", "form": form, "kernel": cls, "level": 0, "achieved": achieved, "peak": hbm,
+             "unit": "GB/s", "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind, "launches": n0,
+             "avg_launch_ms": ms0 / n0, "algorithmic_bytes_per_launch": bytes0,
+             "all_levels": {"launches": prof_f[cls][0], "ms": prof_f[cls][1]}}
+        ratio = NCU_TRAFFIC_RATIO.get((form, key))
+        if ratio:
+            r["traffic"] = bytes0 * ratio
+            r["traffic_source"] = "ncu at 256x256 Q3, scaled by block rows"
+        return r
+
+    _, _, prec_h = FORMS[headline]
+    prof, per_level = profs[headline]
+    cls = max(prof, key=lambda k: prof[k][1])
+    keymap = {"gauss_seidel": "gs", "jacobi": "jacobi", "spmv": "spmv"}
+    roof = kernel_roof(headline, cls, keymap.get(cls)) or {
+        "bound": "hbm", "kernel": cls, "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None, "traffic": None,
+        "peak_kind": peak_kind}
+    roof_more = [r for r in (kernel_roof(f, c, keymap[c]) for f in names for c in ("jacobi", "spmv", "gauss_seidel")
+                             if not (f == headline and c == cls)) if r]
     gpu_launches = int(sum(v[0] for v in prof.values()))
     results[headline]["per_level_ms"] = {k: {str(l): round(v[1] / args.steps, 4) for l, v in d.items()}
                                          for k, d in per_level.items()}
@@ -783,32 +822,45 @@ def run_gpu(args, ws, rank, local):
     if f64 and mx:
         speedup["best_mixed_vs_best_fp64"] = min(f64) / min(mx)
 
+    relax_h = FORMS[headline][0]
+    # compact per-form summary (kept near the end of the line)
+    forms_short = {f: {"ms": round(r["ms"], 3), "iters": r["iters"],
+                       "rel_error_vs_fp64": r.get("rel_error_vs_fp64"), "kernel_ms": r["kernel_ms"]}
+                   for f, r in results.items()}
     line = {
         "metric": METRIC, "value": results[headline]["ms"], "unit": "ms", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": results[headline]["ms"], "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": {1: "f32 V-cycle / f64 CG", 2: "f16-stored level operators, f32 V-cycle / f64 CG"}.get(prec_h, "f64"),
+        "dtype": DTYPE[prec_h],
         "data": f"synthetic: seeded 8-Gaussian forcing (seed {WL['seed']}), homogeneous Dirichlet",
-        "config": {"workload": workload_name(n, P, levels), "form": FORM_TEXT[headline],
-                   "parallelism": "replicas" if ws > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (A is 2.68 GB in FP64, 1.34 GB in FP32)"},
-        "forms": results,
-        "mixed_vs_fp64_speedup": speedup,
+        "config": run_config(n, P, levels, relax_h),
+        "form": FORM_TEXT[headline],
+        "parallelism": "replicas" if ws > 1 else "single GPU",
+        "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 2 * ndof * 8, "d2h_bytes_per_step": ndof * 8,
+                "api": "mgldg_pcg (host buffers, pinned)"},
+        "roofline": roof,
+        "gpu_launches": gpu_launches,
+        "clocks": clk,
+        "roofline_more": roof_more,
+        "per_level_ms": results[headline].pop("per_level_ms"),
         "spmv": {"precision": "fp64", "ms": spmv_ms, "gbs": s64 / (spmv_ms * 1e-3) / 1e9, "bytes": s64,
                  "frac_of_hbm": s64 / (spmv_ms * 1e-3) / 1e9 / hbm,
                  "fp64_tflops": 2 * nnzb * br * br / (spmv_ms * 1e-3) / 1e12,
                  "fp64_peak_tflops_cublas": fp64_tf},
         "setup_ms": {"problem_build": t_build * 1e3, **setup_ms},
-        "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 2 * ndof * 8, "d2h_bytes_per_step": ndof * 8,
-                "api": "mgldg_pcg (host buffers, pinned)"},
-        "roofline": roof,
         "batched": batched,
         "unstructured": unstructured,
         "adjoint": adjoint,
-        "gpu_launches": gpu_launches,
-        "clocks": clk,
+        "forms": forms_short,
+        "mixed_vs_fp64_speedup": speedup,
     }
     return line, results
+
+
+def run_config(n, P, levels, relax):
+    """The workload as both arms name it (the reference arm runs the same
+    problem, smoother and tolerance in FP64 on the host)."""
+    return {"workload": workload_name(n, P, levels), "smoother": SMOOTHER_TEXT[relax], "l2": L2_TEXT}
 
 
 def main():
@@ -819,8 +871,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=WL["n"])
     ap.add_argument("--levels", type=int, default=WL["levels"])
-    ap.add_argument("--forms", default="mixed16_jacobi,mixed_jacobi,fp64_jacobi,mixed_gs,fp64_gs")
-    ap.add_argument("--headline", default="mixed16_jacobi")
+    ap.add_argument("--forms", default="mixed_jacobi,fp64_jacobi,mixed_gs,fp64_gs,mixed16_jacobi")
+    ap.add_argument("--headline", default="mixed_jacobi")
     ap.add_argument("--batched", type=int, default=64, help="right-hand sides of the multi-RHS line (0: skip)")
     ap.add_argument("--batched-n", type=int, default=512, help="mesh side of the uniform multi-RHS mesh")
     ap.add_argument("--batched-mesh", default="adaptive", choices=["adaptive", "uniform"])
@@ -829,32 +881,51 @@ def main():
     ap.add_argument("--disk-batch", type=int, default=48, help="meshes in the uneven batch (0: skip the line)")
     ap.add_argument("--ball-h", type=float, default=0.026, help="tetrahedral ball mesh size of the adjoint line (0: skip)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
+    ap.add_argument("--cpu-smoothers", default="jacobi",
+                    help="smoothers of the CPU oracle's full solves (comma list of jacobi, gs; the first is the "
+                         "reported value)")
+    ap.add_argument("--cpu-oracle", default=None, help=argparse.SUPPRESS)
     ap.add_argument("--vcycle", default="mixed", choices=["mixed16", "mixed"],
                     help="V-cycle form of the unstructured and adjoint lines (their blocks are below 16 x 16, "
                          "which the FP16 copy does not cover)")
     args = ap.parse_args()
+    if args.cpu_oracle is not None:
+        # child process of the CPU baseline: full oracle solves, one JSON line
+        res = [cpu_oracle_solve(args.n, WL["P"], args.levels, sm, WL["tol"], WL["seed"])
+               for sm in args.cpu_oracle.split(",") if sm]
+        print(json.dumps(res), flush=True)
+        return
     ws, rank, local = dist_setup()
     if args.impl == "reference":
+        # the reference's CPU solver (the oracle port), one full solve per
+        # smoother on the host; under torchrun only rank 0 works
         if rank == 0:
-            cb = cpu_baseline(args.n, WL["P"], args.levels, REF_ITERS, WL["tol"], WL["seed"])
-            line = {"metric": METRIC, "value": cb["value"], "unit": "ms", "n_gpus": ws, "steps": 1, "warmup": 0,
-                    "ms_per_step": cb["value"], "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-                    "dtype": "f64", "data": f"synthetic: seeded 8-Gaussian forcing (seed {WL['seed']})",
-                    "config": {"workload": workload_name(args.n, WL["P"], args.levels),
-                               "form": "reference method: FP64 Gauss-Seidel V(2,2), serial CPU"},
+            smoothers = [sm for sm in args.cpu_smoothers.split(",") if sm]
+            res = [cpu_oracle_solve(args.n, WL["P"], args.levels, sm, WL["tol"], WL["seed"]) for sm in smoothers]
+            cb = cpu_baseline_line(res, args.n, WL["P"])
+            v = cb["value"]
+            relax = REF_SMOOTHERS[smoothers[0]][0]
+            line = {"metric": METRIC, "value": v, "unit": "ms", "n_gpus": ws, "steps": 1, "warmup": 0,
+                    "ms_per_step": v, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+                    "dtype": "f64", "data": f"synthetic: seeded 8-Gaussian forcing (seed {WL['seed']}), "
+                                            f"homogeneous Dirichlet",
+                    "config": run_config(args.n, WL["P"], args.levels, relax),
+                    "form": "reference method on the host: FP64 MG-PCG, serial (one full solve per smoother)",
                     "impl": "reference",
                     "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
-                    "e2e": {"value": cb["value"], "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                    "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                    "runs": res}
             print(json.dumps(line), flush=True)
         return
     t0 = time.perf_counter()
+    cpu_proc = start_cpu_baseline(args) if (ws == 1 and not args.no_cpu) else None
     line, results = run_gpu(args, ws, rank, local)
     print(f"[bench] GPU part {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
     if rank == 0:
-        if ws == 1 and not args.no_cpu:
-            iters = results["fp64_gs"]["iters"] if "fp64_gs" in results else REF_ITERS
-            cb = cpu_baseline(args.n, WL["P"], args.levels, iters, WL["tol"], WL["seed"])
-            line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        if cpu_proc is not None:
+            res = finish_cpu_baseline(cpu_proc)
+            if res:
+                line["cpu_baseline"] = cpu_baseline_line(res, args.n, WL["P"])
         print(f"[bench] total {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
         print(json.dumps(line), flush=True)
 

@@ -184,9 +184,12 @@ int mgldg_pcg_dev(mgldg_ctx* ctx, mgldg_mg* mg, const mgldg_bsr* A, const double
  * library holds until the process exits.  Limits: at most 131,072 unknowns
  * and maxit <= 1024 (larger requests return MGLDG_ERR_ARG).  b and x are
  * device pointers owned by the caller.  The first call on each device looks
- * up the array's device address, so make it before any stream capture.  All
+ * up the array's device address, so make it before any stream capture; the
+ * address belongs to the device's primary context, so do not call this entry
+ * point again after resetting the device (cudaDeviceReset).  All
  * calls on a device share the array: calls that overlap on the GPU (other
- * streams, threads or contexts) race and must be serialised by the caller. */
+ * streams, threads or contexts) race and must be serialised by the caller.
+ * Non-finite b or x: MGLDG_ERR_BREAKDOWN with 0 iterations, as mgldg_pcg_dev. */
 int mgldg_cg_noalloc_dev(mgldg_ctx* ctx, const mgldg_bsr* A, const double* b,
                          double* x, double tol, int maxit, int* iters, double* res_hist);
 
@@ -405,6 +408,14 @@ int mgldg_adjoint_l2_dev(mgldg_ctx* ctx, mgldg_mg* mg, const mgldg_ops* ops, con
  * level; nlevels is the number of dependent steps of one sweep. */
 int mgldg_gs_levels(int nbr, const int* row_ptr, const int* col_idx, int reverse,
                     int* level, int* order, int* nlevels);
+/* Level sets of one smoothing pass of nsw (1..7) consecutive sweeps in one
+ * direction, as the GPU runs them in one launch (multigrid.h:202-216 applies
+ * the npre forward or npost reverse sweeps back to back): sweep s of row i,
+ * level[s * nbr + i], follows sweep s of the earlier neighbours and sweep
+ * s - 1 of the later neighbours and of row i itself.  nlevels receives the
+ * number of dependent steps of the whole pass (host only, no GPU needed). */
+int mgldg_gs_pass_levels(int nbr, const int* row_ptr, const int* col_idx, int reverse, int nsw,
+                         int* level, int* nlevels);
 /* Failure-detection self test (no reference counterpart): runs the
  * Gauss-Seidel kernel on a two-row system whose dependency is never
  * released, so its bounded wait expires after timeout_ns.  *status receives

@@ -112,16 +112,16 @@ static void relax(mgldg_mg* m, int i, int n, bool reverse) {
     m->ctx->cur_level = i;
     const T* vals = bsr_vals<T>(L.A);
     const bool f16 = m->p.precision == MGLDG_PREC_MIXED_F16;
+    if (m->p.relaxation == MGLDG_RELAX_GAUSS_SEIDEL) {
+        // the n sweeps run as one dataflow pass (sweep k+1 trails sweep k)
+        gs_sweeps<T>(m->ctx, L.A, vals, LV<T>::D(L), LV<T>::b(L), LV<T>::x(L), L.sched, (T)m->p.omega, reverse, n);
+        return;
+    }
     for (int k = 0; k < n; ++k) {
-        if (m->p.relaxation == MGLDG_RELAX_JACOBI) {
-            if (!(f16 && jacobi_f16_t<T>(m->ctx, L.A, LV<T>::D(L), LV<T>::b(L), LV<T>::x(L), LV<T>::xt(L),
-                                          (T)m->p.omega)))
-                jacobi_sweep<T>(m->ctx, L.A, vals, LV<T>::D(L), LV<T>::b(L), LV<T>::x(L), LV<T>::xt(L),
-                                (T)m->p.omega);
-            std::swap(LV<T>::x(L), LV<T>::xt(L));
-        } else {
-            gs_sweep<T>(m->ctx, L.A, vals, LV<T>::D(L), LV<T>::b(L), LV<T>::x(L), L.sched, (T)m->p.omega, reverse);
-        }
+        if (!(f16 && jacobi_f16_t<T>(m->ctx, L.A, LV<T>::D(L), LV<T>::b(L), LV<T>::x(L), LV<T>::xt(L),
+                                      (T)m->p.omega)))
+            jacobi_sweep<T>(m->ctx, L.A, vals, LV<T>::D(L), LV<T>::b(L), LV<T>::x(L), LV<T>::xt(L), (T)m->p.omega);
+        std::swap(LV<T>::x(L), LV<T>::xt(L));
     }
 }
 
@@ -1016,7 +1016,10 @@ static double* g_cg_scratch_addr[64] = {nullptr};
 
 // Device address of g_cg_scratch on `device` (which must be current).  Host
 // code cannot use the symbol's name as a device pointer; the address is
-// looked up once per device, on the first call made on that device.
+// looked up once per device, on the first call made on that device, in the
+// device's primary context (the one the runtime API uses).  The cached
+// address belongs to that context: a process that resets the device
+// (cudaDeviceReset) after the first call must not call the entry point again.
 static double* cg_scratch(int device) {
     MG_REQUIRE(device >= 0 && device < 64, MGLDG_ERR_ARG, "device index out of range for the scratch table");
     std::lock_guard<std::mutex> lock(g_cg_scratch_mu);
@@ -1068,7 +1071,10 @@ extern "C" int mgldg_cg_noalloc_dev(mgldg_ctx* ctx, const mgldg_bsr* A, const do
     sync(ctx);
     const double tol2 = tol * tol;
     int i = 0;
-    bool broke = false;
+    // a non-finite r.r (NaN or inf in b or x) is a breakdown before the
+    // first iteration, reported as mgldg_pcg_dev reports it
+    bool broke = h.breakdown != 0;
+    if (broke) maxit = 0;
     while (i < maxit && h.delta_new > tol2 * h.delta0) {
         spmv<double>(ctx, A, 1.0, d, 0.0, nullptr, q, d, part, &np);
         {

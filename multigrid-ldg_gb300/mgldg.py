@@ -34,7 +34,7 @@ EXPORTS = [
     "mgldg_mg_vcycle_dev", "mgldg_mg_relax", "mgldg_pcg", "mgldg_pcg_dev", "mgldg_cartesian_create",
     "mgldg_problem_destroy", "mgldg_problem_info", "mgldg_problem_ops", "mgldg_problem_interp",
     "mgldg_problem_rhs_gaussian", "mgldg_problem_rhs_gaussian_dev", "mgldg_prof_enable", "mgldg_prof_reset",
-    "mgldg_prof_query", "mgldg_gs_levels", "mgldg_selftest_wait_timeout", "mgldg_cg_noalloc_dev",
+    "mgldg_prof_query", "mgldg_gs_levels", "mgldg_gs_pass_levels", "mgldg_selftest_wait_timeout", "mgldg_cg_noalloc_dev",
     "mgldg_prof_query_level", "mgldg_cartesian_h_interp", "mgldg_cartesian_p_interp",
     "mgldg_bsr_write_mtx", "mgldg_bsr_read_mtx", "mgldg_problem_write_fun",
     "mgldg_ops_construct_laplacian_kappa", "mgldg_kappa_gradient_dev", "mgldg_adjoint_l2_dev",
@@ -61,6 +61,21 @@ def gs_levels(row_ptr, col_idx, reverse=False):
     if rc:
         raise MgldgError(rc, "gs_levels")
     return lev[:n], order[:n], nl.value
+
+
+def gs_pass_levels(row_ptr, col_idx, nsw, reverse=False):
+    """Host-side levels of an nsw-sweep Gauss-Seidel pass: (level[s, i] as an nsw x n array, nlevels)."""
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int32)
+    ci = np.ascontiguousarray(col_idx, dtype=np.int32)
+    if len(ci) == 0:
+        ci = np.zeros(1, np.int32)
+    n = len(rp) - 1
+    lev = np.zeros(max(1, nsw * n), np.int32)
+    nl = C.c_int()
+    rc = lib().mgldg_gs_pass_levels(n, rp, ci, int(reverse), nsw, lev, C.byref(nl))
+    if rc:
+        raise MgldgError(rc, "gs_pass_levels")
+    return lev[:nsw * n].reshape(nsw, n), nl.value
 
 
 class MgldgError(RuntimeError):
@@ -134,6 +149,7 @@ def lib():
         L.mgldg_prof_reset.argtypes = [vp]
         L.mgldg_prof_query.argtypes = [vp, C.c_int, i64p, C.POINTER(C.c_double)]
         L.mgldg_gs_levels.argtypes = [C.c_int, _ip, _ip, C.c_int, _ip, _ip, ip]
+        L.mgldg_gs_pass_levels.argtypes = [C.c_int, _ip, _ip, C.c_int, C.c_int, _ip, ip]
         L.mgldg_selftest_wait_timeout.argtypes = [vp, C.c_int64, ip]
         L.mgldg_cg_noalloc_dev.argtypes = [vp, vp, vp, vp, C.c_double, C.c_int, ip, _dp]
         L.mgldg_prof_query_level.argtypes = [vp, C.c_int, C.c_int, i64p, C.POINTER(C.c_double)]

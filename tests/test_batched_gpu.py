@@ -51,14 +51,14 @@ def _rhs(pr_seeds, P, n):
 
 
 def assert_history_parity(hg, hr, bnorm):
-    # same count; every ||r_k|| within 1e-12 ||b||; while ||r_k|| > 1e-4 ||b||
+    # same count; every ||r_k|| within 1e-12 ||b||; while ||r_k|| > 1e-3 ||b||
     # also within 1e-10 of itself (further down, rounding differences of a
-    # few 1e-15 ||b|| from the SpMM's summation order, which is not the
+    # few 1e-14 ||b|| from the SpMM's summation order, which is not the
     # single-RHS kernel's, are a larger fraction of ||r_k||)
     assert len(hg) == len(hr)
     assert np.all(np.isfinite(hg))
     assert np.abs(hg - hr).max() <= 1e-12 * bnorm
-    big = hr > 1e-4 * bnorm
+    big = hr > 1e-3 * bnorm
     assert np.max(np.abs(hg - hr)[big] / hr[big]) <= 1e-10
 
 

@@ -108,6 +108,51 @@ def test_gs_levels_respect_sequential_order():
                     assert lev[j] < lev[i]
 
 
+@pytest.mark.parametrize("n", [2, 8, 32, 128])
+@pytest.mark.parametrize("nsw", [1, 2, 3])
+def test_gs_pass_depth_on_morton_grid(n, nsw):
+    # nsw fused sweeps of an n x n Morton grid: sweep s trails sweep s-1 by
+    # two levels, so the pass has 2n - 1 + 2 (nsw - 1) dependent steps
+    rp, ci = morton_pattern(n)
+    for rev in (False, True):
+        lev, nl = mgldg.gs_pass_levels(rp, ci, nsw, reverse=rev)
+        assert nl == 2 * n - 1 + 2 * (nsw - 1)
+        lev1, _, nl1 = mgldg.gs_levels(rp, ci, reverse=rev)
+        assert np.array_equal(lev[0], lev1) and nl1 == 2 * n - 1
+
+
+def test_gs_pass_levels_respect_sweep_dependencies():
+    # random symmetric pattern: sweep s of row i comes after sweep s of its
+    # earlier neighbours and after sweep s-1 of itself and its later ones
+    rng = np.random.default_rng(4)
+    n, nsw = 150, 3
+    pairs = set()
+    for _ in range(400):
+        i, j = rng.integers(0, n, 2)
+        if i != j:
+            pairs.add((i, j)); pairs.add((j, i))
+    rows = [[i] for i in range(n)]
+    for i, j in pairs:
+        rows[i].append(j)
+    rp = np.cumsum([0] + [len(r) for r in rows]).astype(np.int32)
+    ci = np.concatenate([sorted(r) for r in rows]).astype(np.int32)
+    for rev in (False, True):
+        lev, nl = mgldg.gs_pass_levels(rp, ci, nsw, reverse=rev)
+        assert nl == lev.max() + 1
+        for s in range(nsw):
+            for i in range(n):
+                if s > 0:
+                    assert lev[s - 1, i] < lev[s, i]
+                for j in rows[i]:
+                    if j == i:
+                        continue
+                    earlier = j > i if rev else j < i
+                    if earlier:
+                        assert lev[s, j] < lev[s, i]
+                    elif s > 0:
+                        assert lev[s - 1, j] < lev[s, i]
+
+
 def test_context_creation_without_gpu_fails_cleanly():
     try:
         import torch

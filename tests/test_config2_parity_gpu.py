@@ -1,0 +1,95 @@
+"""GPU parity at the sizes of the 512 x 512 Q3 benchmark workload.
+
+The benchmark's solver settings -- Q3 LDG (16 DOF per element),
+tau0 = tauD = 1/h, RATRAT Galerkin hierarchy down to the 4 x 4 grid with a
+dense coarsest inverse, V(2,2), no coarse mean projection, tol 1e-10 -- on
+128 x 128 and 256 x 256 grids with FP64 block Gauss-Seidel (omega 0.8) and
+damped block Jacobi (omega 0.7), and on the full 512 x 512 grid with
+Gauss-Seidel.  The GPU's FP64 MG-PCG must take the oracle's iteration count,
+print every residual norm within 1e-12 ||b|| of the oracle's (pcg,
+krylov.h:22-68, preconditioned by the V-cycle of multigrid.h:361-383) and
+return the solution within 1e-10 relative.  The mixed forms (FP32 V-cycle
+with FP32 or block-scaled FP16 level operators, FP64 outer CG) must reach
+the oracle's FP64 solution within 1e-10 relative at the same tolerance.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import mgldg
+import oracle_py as O
+
+pytestmark = pytest.mark.gpu
+
+P, SEED, TOL = 4, 2001, 1e-10
+SMOOTHERS = {"gs": (mgldg.RELAX_GAUSS_SEIDEL, O.RELAX_GS, 0.8), "jacobi": (mgldg.RELAX_JACOBI, O.RELAX_JACOBI, 0.7)}
+_oracle_cache = {}
+
+
+def _levels(n):
+    return int(math.log2(n)) - 1          # n -> 4: log2(n) - 1 levels
+
+
+def oracle_solve(n, smoother):
+    """The oracle's FP64 MG-PCG on the workload (cached per grid and smoother)."""
+    key = (n, smoother)
+    if key not in _oracle_cache:
+        _, orelax, omega = SMOOTHERS[smoother]
+        pr = O.Problem(P, 1 / n, tau0=n, tauD=n, seed=SEED)
+        omg = O.Multigrid(pr, relaxation=orelax, omega=omega, npre=2, npost=2, solver=O.COARSE_DENSE,
+                          nlevels=_levels(n), mean_project=False)
+        b = pr.rhs()
+        x, h, _ = pr.pcg(b, mg=omg, tol=TOL)
+        _oracle_cache[key] = (x, h, b)
+        del omg, pr
+    return _oracle_cache[key]
+
+
+def gpu_solve(ctx, prob, n, smoother, precision):
+    relax, _, omega = SMOOTHERS[smoother]
+    mg = mgldg.Multigrid(ctx, prob.ops, prob.T, relaxation=relax, omega=omega, npre=2, npost=2,
+                         solver=mgldg.COARSE_DENSE, max_levels=_levels(n), mean_project=0, precision=precision)
+    x, h = mgldg.pcg(ctx, prob.ops.A, prob.rhs_gaussian(SEED), precon=mg, tol=TOL)
+    del mg
+    return x, h
+
+
+def assert_fp64_parity(xg, hg, xr, hr, b):
+    bnorm = np.linalg.norm(b)
+    assert len(hg) == len(hr), (len(hg), len(hr))
+    assert np.all(np.isfinite(hg))
+    assert np.abs(hg - hr).max() <= 1e-12 * bnorm
+    assert np.linalg.norm(xg - xr) <= 1e-10 * np.linalg.norm(xr)
+
+
+@pytest.mark.parametrize("n", [128, 256])
+@pytest.mark.parametrize("smoother", ["gs", "jacobi"])
+def test_fp64_pcg_matches_oracle(ctx, n, smoother):
+    xr, hr, b = oracle_solve(n, smoother)
+    prob = mgldg.CartesianProblem(ctx, P, n, tau0=float(n), tauD=float(n))
+    assert np.abs(prob.rhs_gaussian(SEED) - b).max() <= 1e-13 * np.abs(b).max()
+    xg, hg = gpu_solve(ctx, prob, n, smoother, mgldg.PREC_FP64)
+    assert_fp64_parity(xg, hg, xr, hr, b)
+
+
+@pytest.mark.parametrize("smoother", ["gs", "jacobi"])
+@pytest.mark.parametrize("precision", [mgldg.PREC_MIXED, mgldg.PREC_MIXED_F16])
+def test_mixed_reaches_oracle_solution(ctx, smoother, precision):
+    n = 128
+    xr, hr, b = oracle_solve(n, smoother)
+    prob = mgldg.CartesianProblem(ctx, P, n, tau0=float(n), tauD=float(n))
+    xm, hm = gpu_solve(ctx, prob, n, smoother, precision)
+    assert np.linalg.norm(xm - xr) <= 1e-10 * np.linalg.norm(xr)
+    # the FP32 preconditioner costs at most a few iterations
+    assert len(hm) <= len(hr) + 3
+
+
+def test_fp64_gauss_seidel_512_matches_oracle(ctx):
+    # the benchmark's own grid: 4,194,304 unknowns; the oracle takes minutes
+    n = 512
+    xr, hr, b = oracle_solve(n, "gs")
+    prob = mgldg.CartesianProblem(ctx, P, n, tau0=float(n), tauD=float(n))
+    xg, hg = gpu_solve(ctx, prob, n, "gs", mgldg.PREC_FP64)
+    assert_fp64_parity(xg, hg, xr, hr, b)
+    _oracle_cache.pop((n, "gs"), None)

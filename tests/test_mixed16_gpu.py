@@ -4,7 +4,8 @@ scale per block (entries / block max), arithmetic and vectors in FP32, the
 outer CG in FP64.
 
 The form changes the preconditioner, not the solution: PCG must reach the
-FP64 solution (1e-8 relative) in about as many iterations as the FP32 form.
+FP64 solution (1e-10 relative, solved to a residual of 1e-11) and take about
+as many iterations to 1e-10 as the FP32 form.
 One sweep on its own must equal the FP64 sweep to the FP16 quantisation
 (|error| <= 2^-10 of the largest entry times the block row's sum, checked as
 1e-3 of the result's largest entry) on 16x16 blocks (Q4 on a Cartesian
@@ -28,7 +29,9 @@ def _check_pcg(ctx, prob, mgs, b):
     x64, h64 = mgldg.pcg(ctx, prob.ops.A, b, precon=mgs[mgldg.PREC_FP64], tol=1e-12)
     _, h32 = mgldg.pcg(ctx, prob.ops.A, b, precon=mgs[mgldg.PREC_MIXED], tol=1e-10)
     x16, h16 = mgldg.pcg(ctx, prob.ops.A, b, precon=mgs[mgldg.PREC_MIXED_F16], tol=1e-10)
-    assert np.linalg.norm(x16 - x64) <= 1e-8 * np.linalg.norm(x64)
+    # solved to a residual of 1e-11 the FP16-stored form reaches FP64 to 1e-10
+    x16t, _ = mgldg.pcg(ctx, prob.ops.A, b, precon=mgs[mgldg.PREC_MIXED_F16], tol=1e-11)
+    assert np.linalg.norm(x16t - x64) <= 1e-10 * np.linalg.norm(x64)
     assert len(h16) <= len(h32) + 3
     r = prob.ops.A.mv(x16, alpha=-1.0, beta=1.0, y=b)
     assert np.linalg.norm(r) <= 1e-8 * np.linalg.norm(b)

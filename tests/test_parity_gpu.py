@@ -237,8 +237,12 @@ def test_mixed_precision_reaches_fp64_accuracy(ctx, relax):
     mg32 = mgldg.Multigrid(ctx, prob.ops, prob.T, relaxation=relax, omega=omega, npre=2, npost=2,
                            solver=mgldg.COARSE_DENSE, max_levels=5, precision=mgldg.PREC_MIXED)
     x64, h64 = mgldg.pcg(ctx, prob.ops.A, b, precon=mg64, tol=1e-12)
-    x32, h32 = mgldg.pcg(ctx, prob.ops.A, b, precon=mg32, tol=1e-10)
-    assert np.linalg.norm(x32 - x64) <= 1e-10 * np.linalg.norm(x64) * 10
+    # the FP32 V-cycle does not limit the attainable accuracy: solved to a
+    # residual of 1e-11 the mixed form agrees with FP64 to 1e-10 (at 1e-10
+    # both solutions sit ~1e-10 from the exact one; the 128 x 128 workload
+    # test compares them at that tolerance)
+    x32, h32 = mgldg.pcg(ctx, prob.ops.A, b, precon=mg32, tol=1e-11)
+    assert np.linalg.norm(x32 - x64) <= 1e-10 * np.linalg.norm(x64)
     assert len(h32) <= len(h64) + 5
 
 
