@@ -147,6 +147,60 @@ __device__ __forceinline__ bool read_row(const unsigned long long* xp, int j, un
     }
 }
 
+// Polls several packed rows at once: the rows of the slots in `sel` (a
+// warp-uniform bit mask) are loaded together, one L2 round trip per polling
+// round, until every word of each carries an epoch at or after its target.
+// Warp-uniform result: false if the wait ran out or another waiter gave up.
+template <int W, int MAXE>
+__device__ __forceinline__ bool poll_rows(const unsigned long long* xp, const int (&rows)[MAXE],
+                                          const unsigned (&tgt)[MAXE], unsigned sel,
+                                          unsigned (&v)[MAXE][(W + 31) / 32], GsSync* sync, int64_t timeout_ns,
+                                          int lane) {
+    constexpr int NW = (W + 31) / 32;
+    uint64_t t0 = 0;
+    unsigned it = 0;
+    unsigned pending = sel;
+    while (pending) {
+        unsigned long long u[MAXE][NW];
+        // issue every load of the round before checking any of them
+#pragma unroll
+        for (int q = 0; q < MAXE; ++q)
+            if ((pending >> q) & 1u) {
+                const unsigned long long* row = xp + (size_t)rows[q] * W;
+#pragma unroll
+                for (int k = 0; k < NW; ++k) {
+                    const int w = lane + 32 * k;
+                    u[q][k] = w < W ? ld_relaxed_u64(row + w) : ((unsigned long long)tgt[q] << 32);
+                }
+            }
+        unsigned still = 0;
+#pragma unroll
+        for (int q = 0; q < MAXE; ++q)
+            if ((pending >> q) & 1u) {
+                bool ok = true;
+#pragma unroll
+                for (int k = 0; k < NW; ++k) {
+                    v[q][k] = (unsigned)u[q][k];
+                    ok = ok && (int)((unsigned)(u[q][k] >> 32) - tgt[q]) >= 0;
+                }
+                if (!__all_sync(0xffffffffu, ok)) still |= 1u << q;
+            }
+        pending = still;
+        if (!pending) return true;
+        ++it;
+        if (it == 1) t0 = globaltimer_ns();
+        if ((it & 15u) == 0) {
+            bool stop = *(volatile unsigned*)&sync->err != 0;
+            if (!stop && (int64_t)(globaltimer_ns() - t0) > timeout_ns) {
+                atomicOr(&sync->err, 1u);
+                stop = true;
+            }
+            if (__any_sync(0xffffffffu, stop)) return false;
+        }
+    }
+    return true;
+}
+
 // entry cc of a row read by read_row (every lane of the warp takes part)
 template <class T, int W>
 __device__ __forceinline__ T row_entry(const unsigned (&v)[(W + 31) / 32], int cc) {
@@ -254,34 +308,67 @@ __global__ void __launch_bounds__(WPB * 32)
             if (!read_row<W>(xp, j, earlier ? tgt_new : tgt_old, v, sync, timeout_ns, lane)) failed = true;
         }
         if (failed) break;
-        // ---- neighbours' values at the versions this sweep reads ----
+        // ---- neighbours' values at the versions this sweep reads: first the
+        // later neighbours and the row itself (the previous sweep's values,
+        // usually published long before), then the earlier neighbours (this
+        // sweep's values, the dependency chain); each group is polled as a
+        // batch and summed in column order ----
+        unsigned tg[MAXE + 1];
+        int rw[MAXE + 1];
+        unsigned later_sel = 0, earlier_sel = 0;
 #pragma unroll
         for (int q = 0; q < MAXE; ++q) {
-            const int j = ej[q];
-            if (j < 0 || failed) continue;
-            const bool earlier = reverse ? (j > i) : (j < i);
-            unsigned v[NW];
-            if (!read_row<W>(xp, j, earlier ? tgt_new : tgt_old, v, sync, timeout_ns, lane)) {
-                failed = true;
-                continue;
+            rw[q] = ej[q] < 0 ? i : ej[q];
+            const bool earlier = reverse ? (ej[q] > i) : (ej[q] < i);
+            tg[q] = earlier ? tgt_new : tgt_old;
+            if (ej[q] >= 0) {
+                if (earlier) earlier_sel |= 1u << q;
+                else later_sel |= 1u << q;
             }
+        }
+        rw[MAXE] = i;
+        tg[MAXE] = tgt_old;
+        if (s > 0) later_sel |= 1u << MAXE;
+        unsigned v[MAXE + 1][NW];
+        if (later_sel && !poll_rows<W, MAXE + 1>(xp, rw, tg, later_sel, v, sync, timeout_ns, lane)) failed = true;
+        if (failed) break;
+#pragma unroll
+        for (int q = 0; q < MAXE; ++q) {
+            if (!((later_sel >> q) & 1u)) continue;
 #pragma unroll
             for (int c = 0; c < L::CH; ++c) {
                 const int cc = c0 + c;
-                const T xv = row_entry<T, W>(v, cc < B ? cc : 0);
+                const T xv = row_entry<T, W>(v[q], cc < B ? cc : 0);
                 if (cc < B && active) acc += ech[q][c] * xv;
             }
         }
-        if (ne > MAXE && !failed) {
-            // rows with more waited-for neighbours than registers: the rest
+        if (s > 0) {
+            const T xv = row_entry<T, W>(v[MAXE], active ? r : 0);
+            if (active && sl == 0) xi = xv;
+        }
+        if (earlier_sel && !poll_rows<W, MAXE + 1>(xp, rw, tg, earlier_sel, v, sync, timeout_ns, lane)) failed = true;
+        if (failed) break;
+#pragma unroll
+        for (int q = 0; q < MAXE; ++q) {
+            if (!((earlier_sel >> q) & 1u)) continue;
+#pragma unroll
+            for (int c = 0; c < L::CH; ++c) {
+                const int cc = c0 + c;
+                const T xv = row_entry<T, W>(v[q], cc < B ? cc : 0);
+                if (cc < B && active) acc += ech[q][c] * xv;
+            }
+        }
+        if (ne > MAXE) {
+            // rows with more waited-for neighbours than registers: the rest,
+            // one at a time
             int seen = 0;
             for (int k = k0; k < k1 && !failed; ++k) {
                 const int j = __ldg(col_idx + k);
                 const bool earlier = reverse ? (j > i) : (j < i);
                 if (j == i || (!earlier && s == 0)) continue;
                 if (seen++ < MAXE) continue;
-                unsigned v[NW];
-                if (!read_row<W>(xp, j, earlier ? tgt_new : tgt_old, v, sync, timeout_ns, lane)) {
+                unsigned v1[NW];
+                if (!read_row<W>(xp, j, earlier ? tgt_new : tgt_old, v1, sync, timeout_ns, lane)) {
                     failed = true;
                     break;
                 }
@@ -289,18 +376,9 @@ __global__ void __launch_bounds__(WPB * 32)
 #pragma unroll
                 for (int c = 0; c < L::CH; ++c) {
                     const int cc = c0 + c;
-                    const T xv = row_entry<T, W>(v, cc < B ? cc : 0);
+                    const T xv = row_entry<T, W>(v1, cc < B ? cc : 0);
                     if (cc < B && active) acc += __ldg(a + r * B + cc) * xv;
                 }
-            }
-        }
-        if (s > 0 && !failed) {
-            // the row's own value after the previous sweep
-            unsigned v[NW];
-            if (!read_row<W>(xp, i, tgt_old, v, sync, timeout_ns, lane)) failed = true;
-            else {
-                const T xv = row_entry<T, W>(v, active ? r : 0);
-                if (active && sl == 0) xi = xv;
             }
         }
         if (failed) break;
