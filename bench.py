@@ -251,6 +251,74 @@ def fp64_peak_tflops(torch):
     return 2 * n ** 3 / (best * 1e-3) / 1e12
 
 
+def run_config1(args, ctx, ext, torch, local, ws):
+    """The reference method on the small grid: 32 x 32 uniform quadtree, Q2
+    LDG (9 DOF/element, 9,216 DOF), tau0 = tauD = 32, RATRAT hierarchy
+    32 -> 4 (4 levels) with a dense coarsest inverse, FP64 block
+    Gauss-Seidel (omega 0.8) V(2,2) with the reference's coarse mean
+    projection, MG-PCG to 1e-10.  The operator (3.2 MB) lives in L2, so the
+    line is a latency figure: solves per second, device-timed (b resident)
+    and end to end through mgldg_pcg with host buffers; the oracle's whole
+    solve of the same problem is timed beside it."""
+    import mgldg
+    L = mgldg.lib()
+    n, P, levels, seed = 32, 3, 4, 1001
+    prob = mgldg.CartesianProblem(ctx, P, n, tau0=float(n), tauD=float(n))
+    mg = mgldg.Multigrid(ctx, prob.ops, prob.T, npre=2, npost=2, solver=mgldg.COARSE_DENSE, max_levels=levels,
+                         relaxation=mgldg.RELAX_GAUSS_SEIDEL, omega=0.8)
+    dev = f"cuda:{local}"
+    b = torch.empty(prob.ndof, dtype=torch.float64, device=dev)
+    x = torch.zeros_like(b)
+    torch.cuda.synchronize()
+    ctx.check(L.mgldg_problem_rhs_gaussian_dev(ctx.h, prob.h, seed, C.c_void_p(b.data_ptr())), "rhs")
+    ctx.sync()
+    A = prob.ops.A
+    hist = np.zeros(WL["maxit"])
+    it = C.c_int()
+
+    def solve():
+        with torch.cuda.stream(ext):
+            x.zero_()
+        ctx.check(L.mgldg_pcg_dev(ctx.h, mg.h, A.h, C.c_void_p(b.data_ptr()), C.c_void_p(x.data_ptr()), WL["tol"],
+                                  WL["maxit"], C.byref(it), hist), "pcg")
+
+    for _ in range(max(3, args.warmup)):
+        solve()
+    ctx.sync()
+    nrep = 200
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    for _ in range(nrep):
+        solve()
+    e1.record(ext)
+    e1.synchronize()
+    ms = dist_max(e0.elapsed_time(e1) / nrep, ws)
+    bh = b.cpu().numpy()
+    xh = np.zeros_like(bh)
+    t0 = time.perf_counter()
+    for _ in range(nrep):
+        xh[:] = 0.0
+        mgldg.pcg(ctx, A, bh, x=xh, precon=mg, tol=WL["tol"], maxit=WL["maxit"])
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / nrep
+    out = {"workload": ("32x32 uniform quadtree, Q2 LDG (9,216 DOF), tau0=tauD=32, RATRAT 32->4 (4 levels, dense "
+                        "coarsest, mean projection), FP64 block Gauss-Seidel omega=0.8 V(2,2), tol 1e-10"),
+           "ms_per_solve": ms, "solves_per_s": 1e3 / ms, "e2e_ms_per_solve": e2e_ms, "iters": it.value}
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle_py as O
+        t0 = time.perf_counter()
+        pr = O.Problem(P, 1.0 / n, tau0=n, tauD=n, seed=seed)
+        omg = O.Multigrid(pr, relaxation=O.RELAX_GS, omega=0.8, npre=2, npost=2, solver=O.COARSE_DENSE,
+                          nlevels=levels, mean_project=True)
+        setup_s = time.perf_counter() - t0
+        t1 = time.perf_counter()
+        _, hr, _ = pr.pcg(pr.rhs(), mg=omg, tol=WL["tol"], maxit=WL["maxit"])
+        out["cpu_oracle"] = {"setup_s": setup_s, "solve_ms": (time.perf_counter() - t1) * 1e3, "iters": len(hr),
+                             "cores": 1}
+    del mg, prob, b, x
+    return out
+
+
 def run_batched(args, ctx, ext, torch, local, ws):
     """Many right-hand sides: k seeded 8-Gaussian forcings (seeds 3001..)
     solved together by the block PCG, mixed precision, damped block Jacobi
@@ -598,6 +666,19 @@ def run_adjoint(args, ctx, ext, torch, local, ws):
     ctx.check(L.mgldg_bsr_mv_dev(ctx.h, -1.0, prob.ops.A.h, p_(u), 1.0, p_(r)), "mv")
     ctx.sync()
     rel_res = float(torch.linalg.norm(r) / torch.linalg.norm(b))
+    # the mixed form's gradient against the FP64 one (FP64 V-cycle, tol 1e-12)
+    del mg
+    kw64 = dict(kw, precision=mgldg.PREC_FP64)
+    mg64 = mgldg.Multigrid(ctx, prob.ops, prob.T, **kw64)
+    u64, lam64, dk64 = torch.zeros_like(b), torch.zeros_like(b), torch.zeros_like(dk)
+    loss64 = C.c_double()
+    its64 = (C.c_int * 2)()
+    ctx.check(L.mgldg_adjoint_l2_dev(ctx.h, mg64.h, prob.ops.h, p_(b), p_(uobs), 1e-12, 600, p_(u64), p_(lam64),
+                                     p_(dk64), C.byref(loss64), its64), "adjoint fp64")
+    ctx.sync()
+    g64 = dk64.cpu().numpy()
+    grad_err = float(np.abs(g - g64).max() / np.abs(g64).max())
+    del mg64, u64, lam64, dk64
     out = {
         "workload": (f"unit ball, cubed-sphere hexahedra cut into 24 tetrahedra each, h={h}: {ne:,} tetrahedra, "
                      f"P2 LDG (10 DOF/element, "
@@ -609,8 +690,10 @@ def run_adjoint(args, ctx, ext, torch, local, ws):
         "ms_per_gradient": ms, "forward_iters": int(itp[0]), "adjoint_iters": int(itp[1]),
         "loss": loss.value, "grad_norm": float(np.linalg.norm(g)), "forward_true_rel_residual": rel_res,
         "problem_build_ms": build_ms, "operator_and_mg_setup_ms": setup_ms, "steps": steps,
+        "grad_rel_error_vs_fp64": grad_err, "fp64_loss_rel_diff": abs(loss.value - loss64.value) / loss64.value,
+        "fp64_iters": [int(its64[0]), int(its64[1])],
     }
-    del mg, prob, b, u, lam, uobs, dk, r
+    del prob, b, u, lam, uobs, dk, r
     torch.cuda.empty_cache()
     return out
 
@@ -755,7 +838,9 @@ def run_gpu(args, ws, rank, local):
             return None
         lb = level_bytes(mgs[form], levels - 1, 4 if prec in (1, 2) else 8, f16=prec == 2)
         n0, ms0 = per_level_f[cls][0]
-        bytes0 = lb[0][key]
+        # a Gauss-Seidel launch is a pass of npre (= npost) sweeps, each
+        # reading the level's blocks once
+        bytes0 = lb[0][key] * (WL["npre"] if key == "gs" else 1)
         achieved = bytes0 * n0 / (ms0 * 1e-3) / 1e9
         r = {"bound": "hbm", "form": form, "kernel": cls, "level": 0, "achieved": achieved, "peak": hbm,
              "unit": "GB/s", "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind, "launches": n0,
@@ -804,6 +889,8 @@ def run_gpu(args, ws, rank, local):
     # the unstructured lines run before the multi-RHS line: after the 64-RHS
     # batch (several GB of work space) the uneven batch of disks measured
     # 128-188 ms instead of 105 ms, for reasons not determined
+    config1 = run_config1(args, ctx, ext, torch, local, ws) if args.config1 else None
+    gc.collect()
     unstructured = run_unstructured(args, ctx, ext, torch, local, ws) if args.disk_h > 0 else None
     gc.collect()
     if args.batched > 0:
@@ -848,6 +935,7 @@ def run_gpu(args, ws, rank, local):
                  "fp64_tflops": 2 * nnzb * br * br / (spmv_ms * 1e-3) / 1e12,
                  "fp64_peak_tflops_cublas": fp64_tf},
         "setup_ms": {"problem_build": t_build * 1e3, **setup_ms},
+        "config1": config1,
         "batched": batched,
         "unstructured": unstructured,
         "adjoint": adjoint,
@@ -879,6 +967,7 @@ def main():
     ap.add_argument("--disk-h", type=float, default=0.004, help="mesh size of the single unstructured disk (0: skip "
                     "the unstructured lines)")
     ap.add_argument("--disk-batch", type=int, default=48, help="meshes in the uneven batch (0: skip the line)")
+    ap.add_argument("--config1", type=int, default=1, help="time the 32x32 Q2 reference-method line (0: skip)")
     ap.add_argument("--ball-h", type=float, default=0.026, help="tetrahedral ball mesh size of the adjoint line (0: skip)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
     ap.add_argument("--cpu-smoothers", default="jacobi",

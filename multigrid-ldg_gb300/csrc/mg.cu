@@ -224,6 +224,7 @@ __global__ void k_pcg_init(PcgScalars* sc, const double* partials, int np) {
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sm[w];
         sc->delta_new = t;
         sc->delta0 = t;
+        sc->it = 0;
         // r.z < 0: preconditioner not positive definite; NaN/inf: it failed
         sc->breakdown = (t < 0.0 || !isfinite(t)) ? 1 : 0;
     }
@@ -254,12 +255,13 @@ __global__ void k_pcg_alpha(PcgScalars* sc, const double* partials, int np) {
     }
 }
 
+// it < 0: the iteration index is the device-side counter
 __global__ void k_pcg_rr(PcgScalars* sc, const double* partials, int np, double* hist, int it) {
     __shared__ double sm[32];
     double rr = block_total(partials, np, sm);
     if (threadIdx.x == 0) {
         sc->rr = rr;
-        hist[it] = sqrt(rr);
+        hist[it >= 0 ? it : sc->it] = sqrt(rr);
     }
 }
 
@@ -275,7 +277,18 @@ __global__ void k_pcg_beta(PcgScalars* sc, const double* partials, int np) {
         // error instead of meeting the r.z test spuriously
         if (!isfinite(b) || rs < 0.0) sc->breakdown = 1;
         sc->beta = b;
+        sc->it += 1;
     }
+}
+
+// while-loop condition of a block of PCG iterations: go on while the
+// reference's test (krylov.h:40) holds, no breakdown was seen, maxit is not
+// reached and the next iteration is not a residual-replacement one (those
+// start the next block, after the host has looked at the scalars)
+__global__ void k_pcg_cond(const PcgScalars* sc, double tol2, int maxit, cudaGraphConditionalHandle h) {
+    const int it = sc->it;
+    const bool go = it < maxit && (it % 50) != 0 && sc->delta_new > tol2 * sc->delta0 && !sc->breakdown;
+    cudaGraphSetConditional(h, go ? 1u : 0u);
 }
 
 // x += alpha d ; (r -= alpha q) ; partial r.r
@@ -510,7 +523,13 @@ static void spmv_df64(mgldg_ctx* ctx, const mgldg_bsr* A, const mgldg_mg* m, dou
     check_launch();
 }
 
+static void drop_pcg_graph(mgldg_mg* m) {
+    if (m->pg.exec) cudaGraphExecDestroy(m->pg.exec);
+    m->pg = mgldg_mg::PcgGraph();
+}
+
 static void ensure_pcg(mgldg_mg* m, mgldg_ctx* ctx, int64_t n, int maxit) {
+    if (m->pcg_n != n || m->pcg_maxit < maxit) drop_pcg_graph(m);
     if (m->pcg_n != n) {
         dfree(m->r); dfree(m->d); dfree(m->q); dfree(m->s); dfree(m->dhi); dfree(m->dlo);
         m->dhi = m->dlo = nullptr;
@@ -601,6 +620,143 @@ static void precon(mgldg_mg* m, const double* r, double* s) {
 void mg_precon(mgldg_mg* m, const double* r, double* s) { precon(m, r, s); }
 void mg_take_errors(mgldg_mg* m) { take_errors(m); }
 
+// One PCG iteration (krylov.h:43-61) on the context's stream: q = A d,
+// alpha, x += alpha d with r -= alpha q (or, when `replace`, r = b - A x),
+// ||r|| into the history at the device-side iteration index, s = M(r),
+// delta_new = r.s, beta (which advances the iteration counter), d = s + beta d.
+// `eager`: the preconditioner's launches are issued directly (inside a graph
+// capture) instead of replaying its own graph.
+static void pcg_iteration(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const double* b, double* x, int64_t n,
+                          bool df, int grid_vec, bool replace, bool eager) {
+    double* part = ctx->d_partials;
+    int np = 0;
+    // q = A d ; alpha = delta_new / d.q
+    if (df) spmv_df64(ctx, A, m, part, &np);
+    else spmv<double>(ctx, A, 1.0, m->d, 0.0, nullptr, m->q, m->d, part, &np);
+    {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_pcg_alpha<<<1, 256, 0, ctx->stream>>>(m->sc, part, np);
+    }
+    check_launch();
+    if (replace) {
+        // x += alpha d ; r = b - A x (residual replacement)
+        {
+            Launch L(ctx, MGLDG_K_VECTOR);
+            k_pcg_update<<<grid_vec, 256, 0, ctx->stream>>>(n, m->sc, m->d, m->q, x, m->r, 0, part);
+        }
+        check_launch();
+        spmv<double>(ctx, A, -1.0, x, 1.0, b, m->r, m->r, part, &np);
+    } else {
+        {
+            Launch L(ctx, MGLDG_K_VECTOR);
+            k_pcg_update<<<grid_vec, 256, 0, ctx->stream>>>(n, m->sc, m->d, m->q, x, m->r, 1, part);
+        }
+        check_launch();
+        np = grid_vec;
+    }
+    {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_pcg_rr<<<1, 256, 0, ctx->stream>>>(m->sc, part, np, m->hist, -1);
+    }
+    check_launch();
+    // s = M(r) ; delta_new = r.s ; beta ; d = s + beta d
+    if (eager && !m->L.empty()) vcycle_dev(m, m->r, m->s, true);
+    else precon(m, m->r, m->s);
+    dot_partials<double>(ctx, (int)n, m->r, m->s, part, &np);
+    {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_pcg_beta<<<1, 256, 0, ctx->stream>>>(m->sc, part, np);
+    }
+    check_launch();
+    {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        if (df) k_pcg_dir_split<<<grid_vec, 256, 0, ctx->stream>>>(n, m->sc, m->s, m->d, m->dhi, m->dlo);
+        else k_pcg_dir<<<grid_vec, 256, 0, ctx->stream>>>(n, m->sc, m->s, m->d);
+    }
+    check_launch();
+}
+
+// Captures a block of iterations as one CUDA graph: the residual-replacement
+// iteration, then a device-side while loop (a conditional graph node) over
+// ordinary iterations whose condition k_pcg_cond sets after each one.  The
+// host looks at the scalars once per block (at most every 50 iterations)
+// instead of after every iteration.  Returns false (and stops trying for
+// this multigrid object) if the runtime refuses any step.
+static bool build_pcg_graph(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const double* b, double* x, int64_t n,
+                            bool df, int grid_vec, double tol, int maxit) {
+    drop_pcg_graph(m);
+    int64_t before[MGLDG_K_NCLASS];
+    std::memcpy(before, ctx->launches, sizeof before);
+    cudaGraph_t graph = nullptr;
+    bool ok = true;
+    mgldg_mg::PcgGraph G;
+    const double tol2 = tol * tol;
+    if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    cudaGraph_t body = nullptr;
+    try {
+        pcg_iteration(ctx, m, A, b, x, n, df, grid_vec, true, true);
+        for (int k = 0; k < MGLDG_K_NCLASS; ++k) G.pro_launches[k] = ctx->launches[k] - before[k];
+        cudaStreamCaptureStatus st;
+        cudaGraph_t cg = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        MG_CHECK_CUDA(cudaStreamGetCaptureInfo(ctx->stream, &st, nullptr, &cg, &deps, nullptr, &ndeps));
+        cudaGraphConditionalHandle h;
+        MG_CHECK_CUDA(cudaGraphConditionalHandleCreate(&h, cg, 0, 0));
+        // the loop's first test, then the loop node itself
+        k_pcg_cond<<<1, 1, 0, ctx->stream>>>(m->sc, tol2, maxit, h);
+        check_launch();
+        MG_CHECK_CUDA(cudaStreamGetCaptureInfo(ctx->stream, &st, nullptr, &cg, &deps, nullptr, &ndeps));
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t wnode;
+        MG_CHECK_CUDA(cudaGraphAddNode(&wnode, cg, deps, nullptr, ndeps, &cp));
+        body = cp.conditional.phGraph_out[0];
+        MG_CHECK_CUDA(cudaStreamUpdateCaptureDependencies(ctx->stream, &wnode, nullptr, 1,
+                                                          cudaStreamSetCaptureDependencies));
+        if (cudaStreamEndCapture(ctx->stream, &graph) != cudaSuccess || !graph) ok = false;
+        if (ok) {
+            // the loop body: one ordinary iteration and the next test
+            int64_t b2[MGLDG_K_NCLASS];
+            std::memcpy(b2, ctx->launches, sizeof b2);
+            MG_CHECK_CUDA(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0,
+                                                        cudaStreamCaptureModeThreadLocal));
+            pcg_iteration(ctx, m, A, b, x, n, df, grid_vec, false, true);
+            k_pcg_cond<<<1, 1, 0, ctx->stream>>>(m->sc, tol2, maxit, h);
+            check_launch();
+            cudaGraph_t bg = nullptr;
+            if (cudaStreamEndCapture(ctx->stream, &bg) != cudaSuccess) ok = false;
+            for (int k = 0; k < MGLDG_K_NCLASS; ++k) G.body_launches[k] = ctx->launches[k] - b2[k];
+        }
+    } catch (...) {
+        ok = false;
+        cudaGraph_t junk = nullptr;
+        cudaStreamEndCapture(ctx->stream, &junk);
+        if (junk) cudaGraphDestroy(junk);
+    }
+    if (ok && cudaGraphInstantiate(&G.exec, graph, 0) != cudaSuccess) {
+        G.exec = nullptr;
+        ok = false;
+    }
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    std::memcpy(ctx->launches, before, sizeof before);   // captured, not run
+    if (!ok) return false;
+    G.A = A;
+    G.b = b;
+    G.x = x;
+    G.tol = tol;
+    G.maxit = maxit;
+    m->pg = G;
+    return true;
+}
+
 // pcg on device vectors (krylov.h:22-68)
 static void pcg_dev(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const double* b, double* x, double tol,
                     int maxit, int* iters, double* res_hist) {
@@ -630,50 +786,33 @@ static void pcg_dev(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const doubl
     int i = 0;
     bool broke = m->h_sc->breakdown != 0;
     if (broke) maxit = 0;
+    // blocks of iterations as graphs (per-kernel event timing needs eager launches)
+    const bool use_graph = !ctx->prof && !m->pcg_graph_off;
     while (i < maxit && m->h_sc->delta_new > tol2 * m->h_sc->delta0) {
-        // q = A d ; alpha = delta_new / d.q
-        if (df) spmv_df64(ctx, A, m, part, &np);
-        else spmv<double>(ctx, A, 1.0, m->d, 0.0, nullptr, m->q, m->d, part, &np);
-        {
-            Launch L(ctx, MGLDG_K_VECTOR);
-            k_pcg_alpha<<<1, 256, 0, ctx->stream>>>(m->sc, part, np);
-        }
-        check_launch();
-        if (i % 50 == 0) {
-            // x += alpha d ; r = b - A x (residual replacement)
-            {
-                Launch L(ctx, MGLDG_K_VECTOR);
-                k_pcg_update<<<grid_vec, 256, 0, ctx->stream>>>(n, m->sc, m->d, m->q, x, m->r, 0, part);
+        if (use_graph && !m->pcg_graph_off) {
+            mgldg_mg::PcgGraph& G = m->pg;
+            if (!(G.exec && G.A == A && G.b == b && G.x == x && G.tol == tol && G.maxit == maxit) &&
+                !build_pcg_graph(ctx, m, A, b, x, n, df, grid_vec, tol, maxit))
+                m->pcg_graph_off = true;
+            if (!m->pcg_graph_off && cudaGraphLaunch(m->pg.exec, ctx->stream) != cudaSuccess) {
+                // refused at launch: nothing ran; iterate from the host
+                cudaGetLastError();
+                drop_pcg_graph(m);
+                m->pcg_graph_off = true;
             }
-            check_launch();
-            spmv<double>(ctx, A, -1.0, x, 1.0, b, m->r, m->r, part, &np);
-        } else {
-            {
-                Launch L(ctx, MGLDG_K_VECTOR);
-                k_pcg_update<<<grid_vec, 256, 0, ctx->stream>>>(n, m->sc, m->d, m->q, x, m->r, 1, part);
+            if (!m->pcg_graph_off) {
+                MG_CHECK_CUDA(cudaMemcpyAsync(m->h_sc, m->sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
+                                              ctx->stream));
+                sync(ctx);
+                const int done = m->h_sc->it - i;   // the replacement iteration + the loop's
+                for (int k = 0; k < MGLDG_K_NCLASS; ++k)
+                    ctx->launches[k] += m->pg.pro_launches[k] + (int64_t)(done - 1) * m->pg.body_launches[k];
+                i = m->h_sc->it;
+                if (m->h_sc->breakdown) { broke = true; break; }
+                continue;
             }
-            check_launch();
-            np = grid_vec;
         }
-        {
-            Launch L(ctx, MGLDG_K_VECTOR);
-            k_pcg_rr<<<1, 256, 0, ctx->stream>>>(m->sc, part, np, m->hist, i);
-        }
-        check_launch();
-        // s = M(r) ; delta_new = r.s ; beta ; d = s + beta d
-        precon(m, m->r, m->s);
-        dot_partials<double>(ctx, (int)n, m->r, m->s, part, &np);
-        {
-            Launch L(ctx, MGLDG_K_VECTOR);
-            k_pcg_beta<<<1, 256, 0, ctx->stream>>>(m->sc, part, np);
-        }
-        check_launch();
-        {
-            Launch L(ctx, MGLDG_K_VECTOR);
-            if (df) k_pcg_dir_split<<<grid_vec, 256, 0, ctx->stream>>>(n, m->sc, m->s, m->d, m->dhi, m->dlo);
-            else k_pcg_dir<<<grid_vec, 256, 0, ctx->stream>>>(n, m->sc, m->s, m->d);
-        }
-        check_launch();
+        pcg_iteration(ctx, m, A, b, x, n, df, grid_vec, i % 50 == 0, false);
         MG_CHECK_CUDA(cudaMemcpyAsync(m->h_sc, m->sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost, ctx->stream));
         sync(ctx);
         ++i;
@@ -694,6 +833,7 @@ mgldg_mg::~mgldg_mg() {
     if (ctx) cudaSetDevice(ctx->device);
     for (auto& g : graphs)
         if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (pg.exec) cudaGraphExecDestroy(pg.exec);
     for (auto& L : this->L) {
         if (L.owns_ops) delete L.ops;
         dfree(L.Dinv); dfree(L.Dinv32);

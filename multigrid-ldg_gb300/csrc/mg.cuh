@@ -53,7 +53,9 @@ void mg_take_errors(mgldg_mg* m);
 
 struct PcgScalars {
     double delta_new, delta_old, delta0, alpha, beta, dq, rr, pad;
-    int breakdown, pad2[3];
+    int breakdown;
+    int it;   // completed iterations (advanced on the device)
+    int pad2[2];
 };
 
 }  // namespace mg
@@ -81,6 +83,21 @@ struct mgldg_mg {
     Graph graphs[2];
     int next_graph = 0;
     bool graphs_off = false;
+    // one block of up to 50 PCG iterations (a residual-replacement iteration,
+    // then the others in a device-side while loop) captured as a CUDA graph,
+    // keyed by its operands
+    struct PcgGraph {
+        const mgldg_bsr* A = nullptr;
+        const double* b = nullptr;
+        double* x = nullptr;
+        double tol = 0;
+        int maxit = 0;
+        cudaGraphExec_t exec = nullptr;
+        int64_t pro_launches[MGLDG_K_NCLASS] = {0};    // the replacement iteration
+        int64_t body_launches[MGLDG_K_NCLASS] = {0};   // one loop iteration
+    };
+    PcgGraph pg;
+    bool pcg_graph_off = false;
     mg::Batch* batch = nullptr;   // multi-RHS work space (batched.cu)
     mg::SegWork* seg = nullptr;   // segmented-PCG work space (batched.cu)
     ~mgldg_mg();
