@@ -319,7 +319,7 @@ def run_config1(args, ctx, ext, torch, local, ws):
     return out
 
 
-def run_batched(args, ctx, ext, torch, local, ws):
+def run_batched(args, ctx, ext, torch, local, ws, precision=None):
     """Many right-hand sides: k seeded 8-Gaussian forcings (seeds 3001..)
     solved together by the block PCG, mixed precision, damped block Jacobi
     (omega 0.7), V(2,2).  Mesh: the adaptive quadtree of the multi-RHS
@@ -354,8 +354,9 @@ def run_batched(args, ctx, ext, torch, local, ws):
         B[:, c] = tmp
     torch.cuda.synchronize()
     X = torch.zeros_like(B)
+    prec = mgldg.PREC_MIXED if precision is None else precision
     mg = mgldg.Multigrid(ctx, prob.ops, prob.T, npre=2, npost=2, solver=mgldg.COARSE_DENSE, max_levels=levels,
-                         mean_project=0, relaxation=mgldg.RELAX_JACOBI, omega=0.7, precision=mgldg.PREC_MIXED)
+                         mean_project=0, relaxation=mgldg.RELAX_JACOBI, omega=0.7, precision=prec)
     A = prob.ops.A
     its = np.zeros(k, np.int32)
     hist = np.zeros(WL["maxit"] * k)
@@ -415,8 +416,9 @@ def run_batched(args, ctx, ext, torch, local, ws):
     tiles = [mgldg.batch_tiles(mg, l) for l in range(mg.nlevels)]
     out = {
         "workload": (f"{mesh}, Q2 LDG (9 DOF/element, {ndof:,} DOF), {k} right-hand sides "
-                     f"(seeds 3001..{3000 + k}), RATRAT ({levels} levels, dense coarsest), mixed "
-                     f"precision, block Jacobi omega=0.7, V(2,2), tol 1e-10 per column"),
+                     f"(seeds 3001..{3000 + k}), RATRAT ({levels} levels, dense coarsest), "
+                     f"{'mixed precision with the level products on the tensor cores (3xTF32)' if prec == mgldg.PREC_MIXED_TF32 else 'mixed precision'}, "
+                     f"block Jacobi omega=0.7, V(2,2), tol 1e-10 per column"),
         "problem_build_ms": build_ms,
         "k": k, "ms_per_batch": ms, "solves_per_s": k / (ms * 1e-3), "ms_per_rhs": ms / k,
         "single_rhs_ms": single_ms, "batching_gain": single_ms / (ms / k),
@@ -886,15 +888,15 @@ def run_gpu(args, ws, rank, local):
     del mgs
     import gc
     gc.collect()
-    # the unstructured lines run before the multi-RHS line: after the 64-RHS
-    # batch (several GB of work space) the uneven batch of disks measured
-    # 128-188 ms instead of 105 ms, for reasons not determined
     config1 = run_config1(args, ctx, ext, torch, local, ws) if args.config1 else None
     gc.collect()
-    unstructured = run_unstructured(args, ctx, ext, torch, local, ws) if args.disk_h > 0 else None
-    gc.collect()
+    batched_tc = None
     if args.batched > 0:
         batched = run_batched(args, ctx, ext, torch, local, ws)
+        gc.collect()
+        batched_tc = run_batched(args, ctx, ext, torch, local, ws, precision=mgldg.PREC_MIXED_TF32)
+    gc.collect()
+    unstructured = run_unstructured(args, ctx, ext, torch, local, ws) if args.disk_h > 0 else None
     gc.collect()
     adjoint = run_adjoint(args, ctx, ext, torch, local, ws) if args.ball_h > 0 else None
 
@@ -937,6 +939,7 @@ def run_gpu(args, ws, rank, local):
         "setup_ms": {"problem_build": t_build * 1e3, **setup_ms},
         "config1": config1,
         "batched": batched,
+        "batched_tensor_cores": batched_tc,
         "unstructured": unstructured,
         "adjoint": adjoint,
         "forms": forms_short,

@@ -129,6 +129,10 @@ int mgldg_ops_destroy(mgldg_ops* ops);
                                         residuals reading a block-scaled FP16 copy (one FP32
                                         scale per block) where the blocks are 16 x 16; other
                                         block sizes run as in MIXED */
+#define MGLDG_PREC_MIXED_TF32    3   /* MIXED, with the multi-RHS V-cycle's level-operator
+                                        products (square blocks 4..16) on the tensor cores:
+                                        TF32 operands split in high and low parts (3xTF32),
+                                        FP32 accumulation; single-RHS solves run as MIXED */
 
 /* MG::Parameters (multigrid.h:48-62) plus the build's extensions. */
 typedef struct mgldg_mg_params {

@@ -18,6 +18,7 @@
 // timing every valid candidate once when the work space is set up.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <map>
 
 #include "api.cuh"
@@ -274,7 +275,189 @@ __global__ void __launch_bounds__(256) k_spmm_generic(const SpmmArgs<T> a, int b
 struct TileCfg {
     int V = 1;
     int wpb = 8;
+    bool mma = false;   // tensor-core kernel (k_spmm_mma), MGLDG_PREC_MIXED_TF32 only
 };
+
+// ------------------------------------------------ tensor-core block SpMM --
+// The FP32 multi-RHS products on the tensor pipes: mma.sync m16n8k8 with
+// TF32 operands and FP32 accumulation, each FP32 value split into a high and
+// a low TF32 part (x = hi + lo, lo = tf32(x - hi)) and each product formed as
+// lo*hi + hi*lo + hi*hi ("3xTF32", about 2^-21 relative per product, the
+// accuracy class of FP32).  One warp owns block row i and a tile of 64
+// columns: the b x b block (b <= 16) is the 16 x 16 A operand (rows and
+// columns beyond b are zero), the 64 columns of X_j eight 8-column B
+// operands; the 16 x 64 accumulator tile stays in registers across the row's
+// blocks.  MODE 1 (Jacobi) stages t = B_i - (A X)_i in shared memory and
+// applies Dinv_i with the same split products.
+__device__ __forceinline__ unsigned f2tf32(float x) {
+    unsigned r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ void split_tf32(float x, unsigned& hi, unsigned& lo) {
+    hi = f2tf32(x);
+    lo = f2tf32(x - __uint_as_float(hi));
+}
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const unsigned (&a)[4], const unsigned (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+__device__ __forceinline__ void mma_3xtf32(float (&d)[4], const unsigned (&ah)[4], const unsigned (&al)[4],
+                                           const unsigned (&bh)[2], const unsigned (&bl)[2]) {
+    mma_tf32(d, al, bh);
+    mma_tf32(d, ah, bl);
+    mma_tf32(d, ah, bh);
+}
+
+// A operand rows g, g+8, columns ka = 8 s + t and ka + 4 of a b x b row-major block
+template <int B>
+__device__ __forceinline__ void a_frag(const float* __restrict__ A, int s, int g, int t, unsigned (&ah)[4],
+                                       unsigned (&al)[4]) {
+    const int ka = s * 8 + t, kb = ka + 4;
+    float v[4];
+    v[0] = (g < B && ka < B) ? __ldg(A + g * B + ka) : 0.f;
+    v[1] = (g + 8 < B && ka < B) ? __ldg(A + (g + 8) * B + ka) : 0.f;
+    v[2] = (g < B && kb < B) ? __ldg(A + g * B + kb) : 0.f;
+    v[3] = (g + 8 < B && kb < B) ? __ldg(A + (g + 8) * B + kb) : 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) split_tf32(v[q], ah[q], al[q]);
+}
+
+template <int B, int MODE>
+__global__ void __launch_bounds__(256) k_spmm_mma(const SpmmArgs<float> a) {
+    static_assert(B >= 1 && B <= 16, "tensor-core SpMM takes blocks up to 16 x 16");
+    constexpr int KS = (B + 7) / 8;   // k-steps of 8
+    constexpr int RS = 72;            // row stride of the staged Jacobi tile (conflict-free B reads)
+    __shared__ float tile[8][16 * RS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane >> 2, t = lane & 3;
+    const int k = a.k;
+    const int c0 = blockIdx.y * 64;
+    for (int i = blockIdx.x * 8 + warp; i < a.nbr; i += gridDim.x * 8) {
+        float acc[8][4];
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[nt][q] = 0.f;
+        const int k0 = a.row_ptr[i], k1 = a.row_ptr[i + 1];
+        for (int kk = k0; kk < k1; ++kk) {
+            const float* A = a.val + (size_t)(a.blk ? a.blk[kk] : kk) * (B * B);
+            const float* xb = a.X + (size_t)a.col_idx[kk] * B * k;
+#pragma unroll
+            for (int s = 0; s < KS; ++s) {
+                unsigned ah[4], al[4];
+                a_frag<B>(A, s, g, t, ah, al);
+                const int ka = s * 8 + t, kb = ka + 4;
+#pragma unroll
+                for (int nt = 0; nt < 8; ++nt) {
+                    const int col = c0 + nt * 8 + g;
+                    const float x0 = (ka < B && col < k) ? __ldg(xb + (size_t)ka * k + col) : 0.f;
+                    const float x1 = (kb < B && col < k) ? __ldg(xb + (size_t)kb * k + col) : 0.f;
+                    unsigned bh[2], bl[2];
+                    split_tf32(x0, bh[0], bl[0]);
+                    split_tf32(x1, bh[1], bl[1]);
+                    mma_3xtf32(acc[nt], ah, al, bh, bl);
+                }
+            }
+        }
+        const size_t y0 = (size_t)i * B * k;
+        if constexpr (MODE == 0) {
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) {
+                        const int row = g + 8 * h, col = c0 + nt * 8 + 2 * t + e;
+                        if (row < B && col < k) {
+                            const size_t idx = y0 + (size_t)row * k + col;
+                            float v = a.alpha * acc[nt][2 * h + e];
+                            if (a.beta != 0.f) v += a.beta * a.Yin[idx];
+                            a.Y[idx] = v;
+                        }
+                    }
+        } else {
+            // t = B_i - (A X)_i into the warp's tile (rows >= b are zero)
+            float* T = tile[warp];
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) {
+                        const int row = g + 8 * h, cl = nt * 8 + 2 * t + e, col = c0 + cl;
+                        float v = 0.f;
+                        if (row < B && col < k) v = a.B[y0 + (size_t)row * k + col] - acc[nt][2 * h + e];
+                        T[row * RS + cl] = v;
+                    }
+            __syncwarp();
+            float out[8][4];
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) out[nt][q] = 0.f;
+            const float* D = a.Dinv + (size_t)i * B * B;
+#pragma unroll
+            for (int s = 0; s < KS; ++s) {
+                unsigned ah[4], al[4];
+                a_frag<B>(D, s, g, t, ah, al);
+                const int ka = s * 8 + t, kb = ka + 4;
+#pragma unroll
+                for (int nt = 0; nt < 8; ++nt) {
+                    unsigned bh[2], bl[2];
+                    split_tf32(T[ka * RS + nt * 8 + g], bh[0], bl[0]);
+                    split_tf32(T[kb * RS + nt * 8 + g], bh[1], bl[1]);
+                    mma_3xtf32(out[nt], ah, al, bh, bl);
+                }
+            }
+            __syncwarp();
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) {
+                        const int row = g + 8 * h, col = c0 + nt * 8 + 2 * t + e;
+                        if (row < B && col < k) {
+                            const size_t idx = y0 + (size_t)row * k + col;
+                            a.Y[idx] = a.X[idx] + a.omega * out[nt][2 * h + e];
+                        }
+                    }
+        }
+    }
+}
+
+static bool mma_shape(int br, int bc) { return br == bc && (br == 4 || br == 6 || br == 9 || br == 10 || br == 16); }
+
+template <int B, int MODE>
+static void launch_mma(mgldg_ctx* ctx, const SpmmArgs<float>& a, int kclass) {
+    const int ncolt = (a.k + 63) / 64;
+    int per_sm = 0;
+    MG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spmm_mma<B, MODE>, 256, 0));
+    per_sm = std::max(1, per_sm);
+    const int want = (a.nbr + 7) / 8;
+    const int gx = std::max(1, std::min(want, ctx->sm_count * per_sm * 4 / std::max(1, ncolt) + 1));
+    {
+        Launch L(ctx, kclass);
+        k_spmm_mma<B, MODE><<<dim3(gx, ncolt), 256, 0, ctx->stream>>>(a);
+    }
+    check_launch();
+}
+
+static void spmm_mma(mgldg_ctx* ctx, int b, const SpmmArgs<float>& a, int mode, int kclass) {
+#define MG_M(B)                                             \
+    if (b == B) {                                           \
+        if (mode == 0) launch_mma<B, 0>(ctx, a, kclass);   \
+        else launch_mma<B, 1>(ctx, a, kclass);             \
+        return;                                             \
+    }
+    MG_M(4) MG_M(6) MG_M(9) MG_M(10) MG_M(16)
+#undef MG_M
+    throw Error(MGLDG_ERR_UNSUPPORTED, "tensor-core SpMM: unsupported block size");
+}
 
 template <class T, int BR, int BC, int V, int MODE>
 static void launch_tiled(mgldg_ctx* ctx, const SpmmArgs<T>& a, int wpb, int kclass) {
@@ -326,6 +509,12 @@ static bool tile_valid(const SpmmArgs<T>& a, int V) {
 template <class T>
 static void spmm_launch(mgldg_ctx* ctx, int br, int bc, const SpmmArgs<T>& a, int mode, TileCfg cfg, int kclass) {
     if (a.nbr == 0 || a.k == 0) return;
+    if constexpr (sizeof(T) == 4) {
+        if (cfg.mma && mma_shape(br, bc)) {
+            spmm_mma(ctx, br, a, mode, kclass);
+            return;
+        }
+    }
     if (is_tiled_shape(br, bc) && tile_valid(a, cfg.V)) {
         bool ok = false;
 #define MG_B(B)                                                                                        \
@@ -375,9 +564,22 @@ __global__ void __launch_bounds__(256) k_coldot(int64_t n, int k, const T* __res
     const int rp = max(1, 256 / kc);          // rows per pass
     const int col = c0 + threadIdx.x % kc, ro = threadIdx.x / kc;
     double s = 0;
-    if (ro < rp)
-        for (int64_t u = (int64_t)blockIdx.x * rp + ro; u < n; u += (int64_t)gridDim.x * rp)
-            s += (double)a[u * k + col] * (double)b[u * k + col];
+    if (ro < rp) {
+        // four rows per round: their loads are in flight together
+        const int64_t step = (int64_t)gridDim.x * rp;
+        int64_t u = (int64_t)blockIdx.x * rp + ro;
+        for (; u + 3 * step < n; u += 4 * step) {
+            const double p0 = (double)a[u * k + col] * (double)b[u * k + col];
+            const double p1 = (double)a[(u + step) * k + col] * (double)b[(u + step) * k + col];
+            const double p2 = (double)a[(u + 2 * step) * k + col] * (double)b[(u + 2 * step) * k + col];
+            const double p3 = (double)a[(u + 3 * step) * k + col] * (double)b[(u + 3 * step) * k + col];
+            s += p0;
+            s += p1;
+            s += p2;
+            s += p3;
+        }
+        for (; u < n; u += step) s += (double)a[u * k + col] * (double)b[u * k + col];
+    }
     sm[threadIdx.x] = s;
     __syncthreads();
     if ((int)threadIdx.x < kc) {
@@ -388,7 +590,7 @@ __global__ void __launch_bounds__(256) k_coldot(int64_t n, int k, const T* __res
 }
 
 static int coldot_grid(mgldg_ctx* ctx, int64_t n) {
-    return (int)std::max<int64_t>(1, std::min<int64_t>(n / 8 + 1, ctx->sm_count * 2));
+    return (int)std::max<int64_t>(1, std::min<int64_t>(n / 8 + 1, ctx->sm_count * 4));
 }
 
 template <class T>
@@ -407,7 +609,8 @@ static void coldot(mgldg_ctx* ctx, int64_t n, int k, const T* a, const T* b, dou
 struct BatchScalars {
     double *delta_new, *delta_old, *delta0, *alpha, *beta;
     int *active, *iters, *broken;
-    int* counter;   // [0] = active columns after the iteration, [1] = broken
+    int* counter;   // [0] = active columns after the iteration, [1] = broken,
+                    // [2] = completed iterations (segmented PCG only)
 };
 
 __device__ double col_total(const double* partials, int np, int k, int c) {
@@ -461,8 +664,11 @@ __global__ void k_bpcg_alpha(int k, BatchScalars sc, const double* partials, int
 __global__ void __launch_bounds__(256) k_bpcg_update(int64_t nk, int k, BatchScalars sc, const double* __restrict__ d,
                                                      const double* __restrict__ q, double* __restrict__ x,
                                                      double* __restrict__ r, int update_r) {
-    for (int64_t e = (int64_t)blockIdx.x * 256 + threadIdx.x; e < nk; e += (int64_t)gridDim.x * 256) {
-        const int c = (int)(e % k);
+    const int64_t stride = (int64_t)gridDim.x * 256;
+    const int dc = (int)(stride % k);
+    int64_t e = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    int c = (int)(e % k);
+    for (; e < nk; e += stride, c = (c + dc >= k) ? c + dc - k : c + dc) {
         if (!sc.active[c]) continue;
         const double al = sc.alpha[c];
         x[e] += al * d[e];
@@ -470,10 +676,11 @@ __global__ void __launch_bounds__(256) k_bpcg_update(int64_t nk, int k, BatchSca
     }
 }
 
+// it < 0: the iteration index is the device-side counter[2]
 __global__ void k_bpcg_rr(int k, BatchScalars sc, const double* partials, int np, double* hist, int maxit, int it) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= k || !sc.active[c]) return;
-    hist[(size_t)c * maxit + it] = sqrt(col_total(partials, np, k, c));
+    hist[(size_t)c * maxit + (it >= 0 ? it : sc.counter[2])] = sqrt(col_total(partials, np, k, c));
 }
 
 __global__ void k_bpcg_beta(int k, BatchScalars sc, const double* partials, int np) {
@@ -497,14 +704,18 @@ __global__ void k_bpcg_beta(int k, BatchScalars sc, const double* partials, int 
 // d = s + beta d (active columns)
 __global__ void __launch_bounds__(256) k_bpcg_dir(int64_t nk, int k, BatchScalars sc, const double* __restrict__ s,
                                                   double* __restrict__ d) {
-    for (int64_t e = (int64_t)blockIdx.x * 256 + threadIdx.x; e < nk; e += (int64_t)gridDim.x * 256) {
-        const int c = (int)(e % k);
+    const int64_t stride = (int64_t)gridDim.x * 256;
+    const int dc = (int)(stride % k);
+    int64_t e = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    int c = (int)(e % k);
+    for (; e < nk; e += stride, c = (c + dc >= k) ? c + dc - k : c + dc) {
         if (sc.active[c]) d[e] = s[e] + sc.beta[c] * d[e];
     }
 }
 
 __global__ void k_bpcg_end(int k, BatchScalars sc, double tol2, int maxit, int it) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (it < 0) it = sc.counter[2];
     if (c >= k || !sc.active[c]) return;
     sc.iters[c] = it + 1;
     sc.active[c] = (it + 1 < maxit && sc.delta_new[c] > tol2 * sc.delta0[c]) ? 1 : 0;
@@ -726,7 +937,7 @@ static void ensure_batch(mgldg_mg* m, int k, const mgldg_bsr* A_outer) {
         b->sc.broken = b->sc_int + 2 * k;
         b->sc.counter = b->sc_int + 3 * k;
         MG_CHECK_CUDA(cudaMallocHost(&b->h_counter, 2 * sizeof(int)));
-        b->partials_len = ctx->sm_count * 2 * k;
+        b->partials_len = ctx->sm_count * 4 * k;   // coldot_grid partial rows per column
         b->partials = dalloc<double>(b->partials_len);
     }
     Batch* b = m->batch;
@@ -738,9 +949,15 @@ static void ensure_batch(mgldg_mg* m, int k, const mgldg_bsr* A_outer) {
             LevelData& L = m->L[l];
             BatchLevel& B = b->L[l];
             if (mixed) {
-                B.spmm = autotune<float>(ctx, L.A, bsr_vals<float>(L.A), k, 0, B.x32, B.r32, nullptr, nullptr);
-                if (L.Dinv32)
-                    B.jac = autotune<float>(ctx, L.A, bsr_vals<float>(L.A), k, 1, B.x32, B.xt32, L.Dinv32, B.b32);
+                if (m->p.precision == MGLDG_PREC_MIXED_TF32 && !L.A->blk && mma_shape(L.A->br, L.A->bc)) {
+                    // the level operator's products on the tensor pipes (no
+                    // timing choice: the form fixes the arithmetic)
+                    B.spmm.mma = B.jac.mma = true;
+                } else {
+                    B.spmm = autotune<float>(ctx, L.A, bsr_vals<float>(L.A), k, 0, B.x32, B.r32, nullptr, nullptr);
+                    if (L.Dinv32)
+                        B.jac = autotune<float>(ctx, L.A, bsr_vals<float>(L.A), k, 1, B.x32, B.xt32, L.Dinv32, B.b32);
+                }
                 if (l + 1 < m->L.size()) {
                     BatchLevel& C = b->L[l + 1];
                     B.restrict_ = autotune<float>(ctx, L.Tt, bsr_vals<float>(L.Tt), k, 0, B.r32, C.b32, nullptr, nullptr);
@@ -993,8 +1210,11 @@ __global__ void __launch_bounds__(256) k_bsplit(int64_t nk, const double* __rest
 __global__ void __launch_bounds__(256) k_bpcg_dir_split(int64_t nk, int k, BatchScalars sc, const double* __restrict__ s,
                                                         double* __restrict__ d, float* __restrict__ hi,
                                                         float* __restrict__ lo) {
-    for (int64_t e = (int64_t)blockIdx.x * 256 + threadIdx.x; e < nk; e += (int64_t)gridDim.x * 256) {
-        const int c = (int)(e % k);
+    const int64_t stride = (int64_t)gridDim.x * 256;
+    const int dc = (int)(stride % k);
+    int64_t e = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    int c = (int)(e % k);
+    for (; e < nk; e += stride, c = (c + dc >= k) ? c + dc - k : c + dc) {
         if (sc.active[c]) {
             const double v = s[e] + sc.beta[c] * d[e];
             d[e] = v;
@@ -1199,10 +1419,21 @@ struct SegWork {
     double* sc_mem = nullptr;
     int* sc_int = nullptr;
     int* h_counter = nullptr;
+    // blocks of up to 50 iterations as one CUDA graph (as in pcg_dev),
+    // keyed by the operands
+    cudaGraphExec_t exec = nullptr;
+    const mgldg_bsr* gA = nullptr;
+    const double* gb = nullptr;
+    double* gx_ = nullptr;
+    double gtol = 0;
+    int gmaxit = 0;
+    int64_t pro_launches[MGLDG_K_NCLASS] = {0}, body_launches[MGLDG_K_NCLASS] = {0};
+    bool graph_off = false;
 };
 
 void seg_free(SegWork* w) {
     if (!w) return;
+    if (w->exec) cudaGraphExecDestroy(w->exec);
     dfree(w->off);
     dfree(w->R); dfree(w->D); dfree(w->Q); dfree(w->S); dfree(w->hist); dfree(w->partials);
     dfree(w->sc_mem);
@@ -1277,7 +1508,7 @@ static SegWork* ensure_seg(mgldg_mg* m, const std::vector<int64_t>& off, int max
         w->R = dalloc<double>(n); w->D = dalloc<double>(n); w->Q = dalloc<double>(n); w->S = dalloc<double>(n);
         w->partials = dalloc<double>((size_t)w->gx * nseg);
         w->sc_mem = dalloc<double>(5 * (size_t)nseg);
-        w->sc_int = dalloc<int>(3 * (size_t)nseg + 2);
+        w->sc_int = dalloc<int>(3 * (size_t)nseg + 3);
         w->sc.delta_new = w->sc_mem;
         w->sc.delta_old = w->sc_mem + nseg;
         w->sc.delta0 = w->sc_mem + 2 * nseg;
@@ -1287,10 +1518,14 @@ static SegWork* ensure_seg(mgldg_mg* m, const std::vector<int64_t>& off, int max
         w->sc.iters = w->sc_int + nseg;
         w->sc.broken = w->sc_int + 2 * nseg;
         w->sc.counter = w->sc_int + 3 * nseg;
-        MG_CHECK_CUDA(cudaMallocHost(&w->h_counter, 2 * sizeof(int)));
+        MG_CHECK_CUDA(cudaMallocHost(&w->h_counter, 3 * sizeof(int)));
     }
     upload(ctx, w->off, off.data(), off.size());
     const int len = std::max(1, maxit) * nseg;
+    if (w->hist_len < len && w->exec) {
+        cudaGraphExecDestroy(w->exec);   // bakes the old history buffer
+        w->exec = nullptr;
+    }
     if (w->hist_len < len) {
         dfree(w->hist);
         w->hist = nullptr;
@@ -1298,6 +1533,145 @@ static SegWork* ensure_seg(mgldg_mg* m, const std::vector<int64_t>& off, int max
         w->hist_len = len;
     }
     return w;
+}
+
+__global__ void k_seg_advance(BatchScalars sc) { sc.counter[2] += 1; }
+
+// while-loop condition of a block of segmented iterations: some segment is
+// still active and the next iteration is not a residual-replacement one
+__global__ void k_seg_cond(BatchScalars sc, cudaGraphConditionalHandle h) {
+    cudaGraphSetConditional(h, (sc.counter[0] > 0 && (sc.counter[2] % 50) != 0) ? 1u : 0u);
+}
+
+// one iteration of every active segment's pcg (krylov.h:43-61); `it` < 0:
+// the iteration index is the device-side counter (graph capture)
+static void seg_iteration(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, SegWork* w, const double* b, double* x,
+                          double tol2, int maxit, bool replace, int it, bool eager) {
+    const int nseg = w->nseg;
+    BatchScalars sc = w->sc;
+    const dim3 grid(w->gx, nseg);
+    const int gk = (nseg + 127) / 128;
+    auto segdot = [&](const double* a, const double* c) {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_segdot<<<grid, 256, 0, ctx->stream>>>(w->off, nseg, a, c, w->partials);
+    };
+    spmv<double>(ctx, A, 1.0, w->D, 0.0, nullptr, w->Q);
+    segdot(w->D, w->Q);
+    {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_bpcg_alpha<<<gk, 128, 0, ctx->stream>>>(nseg, sc, w->partials, w->gx);
+    }
+    {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_segupdate<<<grid, 256, 0, ctx->stream>>>(w->off, sc, w->D, w->Q, x, w->R, replace ? 0 : 1);
+    }
+    check_launch();
+    if (replace) spmv<double>(ctx, A, -1.0, x, 1.0, b, w->R);
+    segdot(w->R, w->R);
+    {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_bpcg_rr<<<gk, 128, 0, ctx->stream>>>(nseg, sc, w->partials, w->gx, w->hist, maxit, it);
+    }
+    check_launch();
+    if (eager) mg_precon_eager(m, w->R, w->S);
+    else mg_precon(m, w->R, w->S);
+    segdot(w->R, w->S);
+    {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_bpcg_beta<<<gk, 128, 0, ctx->stream>>>(nseg, sc, w->partials, w->gx);
+    }
+    {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_segdir<<<grid, 256, 0, ctx->stream>>>(w->off, sc, w->S, w->D);
+    }
+    {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_bpcg_end<<<gk, 128, 0, ctx->stream>>>(nseg, sc, tol2, maxit, it);
+    }
+    {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_bpcg_count<<<1, 256, 0, ctx->stream>>>(nseg, sc);
+    }
+    {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_seg_advance<<<1, 1, 0, ctx->stream>>>(sc);
+    }
+    check_launch();
+}
+
+// A block of segmented iterations as one CUDA graph: the residual-replacement
+// iteration, then a conditional while node over ordinary iterations.
+static bool build_seg_graph(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, SegWork* w, const double* b, double* x,
+                            double tol, int maxit) {
+    if (w->exec) {
+        cudaGraphExecDestroy(w->exec);
+        w->exec = nullptr;
+    }
+    const double tol2 = tol * tol;
+    int64_t before[MGLDG_K_NCLASS];
+    std::memcpy(before, ctx->launches, sizeof before);
+    cudaGraph_t graph = nullptr;
+    bool ok = true;
+    if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    try {
+        seg_iteration(ctx, m, A, w, b, x, tol2, maxit, true, -1, true);
+        for (int k = 0; k < MGLDG_K_NCLASS; ++k) w->pro_launches[k] = ctx->launches[k] - before[k];
+        cudaStreamCaptureStatus st;
+        cudaGraph_t cg = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        MG_CHECK_CUDA(cudaStreamGetCaptureInfo(ctx->stream, &st, nullptr, &cg, &deps, nullptr, &ndeps));
+        cudaGraphConditionalHandle h;
+        MG_CHECK_CUDA(cudaGraphConditionalHandleCreate(&h, cg, 0, 0));
+        k_seg_cond<<<1, 1, 0, ctx->stream>>>(w->sc, h);
+        check_launch();
+        MG_CHECK_CUDA(cudaStreamGetCaptureInfo(ctx->stream, &st, nullptr, &cg, &deps, nullptr, &ndeps));
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t wnode;
+        MG_CHECK_CUDA(cudaGraphAddNode(&wnode, cg, deps, nullptr, ndeps, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        MG_CHECK_CUDA(cudaStreamUpdateCaptureDependencies(ctx->stream, &wnode, nullptr, 1,
+                                                          cudaStreamSetCaptureDependencies));
+        if (cudaStreamEndCapture(ctx->stream, &graph) != cudaSuccess || !graph) ok = false;
+        if (ok) {
+            int64_t b2[MGLDG_K_NCLASS];
+            std::memcpy(b2, ctx->launches, sizeof b2);
+            MG_CHECK_CUDA(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0,
+                                                        cudaStreamCaptureModeThreadLocal));
+            seg_iteration(ctx, m, A, w, b, x, tol2, maxit, false, -1, true);
+            k_seg_cond<<<1, 1, 0, ctx->stream>>>(w->sc, h);
+            check_launch();
+            cudaGraph_t bg = nullptr;
+            if (cudaStreamEndCapture(ctx->stream, &bg) != cudaSuccess) ok = false;
+            for (int k = 0; k < MGLDG_K_NCLASS; ++k) w->body_launches[k] = ctx->launches[k] - b2[k];
+        }
+    } catch (...) {
+        ok = false;
+        cudaGraph_t junk = nullptr;
+        cudaStreamEndCapture(ctx->stream, &junk);
+        if (junk) cudaGraphDestroy(junk);
+    }
+    if (ok && cudaGraphInstantiate(&w->exec, graph, 0) != cudaSuccess) {
+        w->exec = nullptr;
+        ok = false;
+    }
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    std::memcpy(ctx->launches, before, sizeof before);   // captured, not run
+    if (!ok) return false;
+    w->gA = A;
+    w->gb = b;
+    w->gx_ = x;
+    w->gtol = tol;
+    w->gmaxit = maxit;
+    return true;
 }
 
 static void segpcg(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const std::vector<int64_t>& off, const double* b,
@@ -1308,14 +1682,13 @@ static void segpcg(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const std::v
     const dim3 grid(w->gx, nseg);
     const int gk = (nseg + 127) / 128;
     const double tol2 = tol * tol;
-    auto segdot = [&](const double* a, const double* c) {
-        Launch L(ctx, MGLDG_K_VECTOR);
-        k_segdot<<<grid, 256, 0, ctx->stream>>>(w->off, nseg, a, c, w->partials);
-    };
     // R = b - A x ; D = M(R) ; delta = R.D per segment
     spmv<double>(ctx, A, -1.0, x, 1.0, b, w->R);
     mg_precon(m, w->R, w->D);
-    segdot(w->R, w->D);
+    {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_segdot<<<grid, 256, 0, ctx->stream>>>(w->off, nseg, w->R, w->D, w->partials);
+    }
     check_launch();
     {
         Launch L(ctx, MGLDG_K_VECTOR);
@@ -1326,50 +1699,37 @@ static void segpcg(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const std::v
         k_bpcg_count<<<1, 256, 0, ctx->stream>>>(nseg, sc);
     }
     check_launch();
-    MG_CHECK_CUDA(cudaMemcpyAsync(w->h_counter, sc.counter, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    MG_CHECK_CUDA(cudaMemsetAsync(sc.counter + 2, 0, sizeof(int), ctx->stream));
+    MG_CHECK_CUDA(cudaMemcpyAsync(w->h_counter, sc.counter, 3 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     sync(ctx);
     mg_take_errors(m);
     int i = 0;
+    static const bool host_loop = std::getenv("MGLDG_PCG_HOST_LOOP") != nullptr;
+    const bool use_graph = !ctx->prof && !w->graph_off && !host_loop;
     while (w->h_counter[0] > 0) {
-        spmv<double>(ctx, A, 1.0, w->D, 0.0, nullptr, w->Q);
-        segdot(w->D, w->Q);
-        {
-            Launch L(ctx, MGLDG_K_VECTOR);
-            k_bpcg_alpha<<<gk, 128, 0, ctx->stream>>>(nseg, sc, w->partials, w->gx);
+        if (use_graph && !w->graph_off) {
+            if (!(w->exec && w->gA == A && w->gb == b && w->gx_ == x && w->gtol == tol && w->gmaxit == maxit) &&
+                !build_seg_graph(ctx, m, A, w, b, x, tol, maxit))
+                w->graph_off = true;
+            if (!w->graph_off && cudaGraphLaunch(w->exec, ctx->stream) != cudaSuccess) {
+                cudaGetLastError();
+                cudaGraphExecDestroy(w->exec);
+                w->exec = nullptr;
+                w->graph_off = true;
+            }
+            if (!w->graph_off) {
+                MG_CHECK_CUDA(cudaMemcpyAsync(w->h_counter, sc.counter, 3 * sizeof(int), cudaMemcpyDeviceToHost,
+                                              ctx->stream));
+                sync(ctx);
+                const int done = w->h_counter[2] - i;
+                for (int k = 0; k < MGLDG_K_NCLASS; ++k)
+                    ctx->launches[k] += w->pro_launches[k] + (int64_t)(done - 1) * w->body_launches[k];
+                i = w->h_counter[2];
+                continue;
+            }
         }
-        const bool replace = i % 50 == 0;
-        {
-            Launch L(ctx, MGLDG_K_VECTOR);
-            k_segupdate<<<grid, 256, 0, ctx->stream>>>(w->off, sc, w->D, w->Q, x, w->R, replace ? 0 : 1);
-        }
-        check_launch();
-        if (replace) spmv<double>(ctx, A, -1.0, x, 1.0, b, w->R);
-        segdot(w->R, w->R);
-        {
-            Launch L(ctx, MGLDG_K_VECTOR);
-            k_bpcg_rr<<<gk, 128, 0, ctx->stream>>>(nseg, sc, w->partials, w->gx, w->hist, maxit, i);
-        }
-        check_launch();
-        mg_precon(m, w->R, w->S);
-        segdot(w->R, w->S);
-        {
-            Launch L(ctx, MGLDG_K_VECTOR);
-            k_bpcg_beta<<<gk, 128, 0, ctx->stream>>>(nseg, sc, w->partials, w->gx);
-        }
-        {
-            Launch L(ctx, MGLDG_K_VECTOR);
-            k_segdir<<<grid, 256, 0, ctx->stream>>>(w->off, sc, w->S, w->D);
-        }
-        {
-            Launch L(ctx, MGLDG_K_VECTOR);
-            k_bpcg_end<<<gk, 128, 0, ctx->stream>>>(nseg, sc, tol2, maxit, i);
-        }
-        {
-            Launch L(ctx, MGLDG_K_VECTOR);
-            k_bpcg_count<<<1, 256, 0, ctx->stream>>>(nseg, sc);
-        }
-        check_launch();
-        MG_CHECK_CUDA(cudaMemcpyAsync(w->h_counter, sc.counter, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        seg_iteration(ctx, m, A, w, b, x, tol2, maxit, i % 50 == 0, i, false);
+        MG_CHECK_CUDA(cudaMemcpyAsync(w->h_counter, sc.counter, 3 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         sync(ctx);
         ++i;
     }

@@ -186,8 +186,43 @@ static void take_errors(mgldg_mg* m) {
     take_device_error(m->ctx);
 }
 
-// one V-cycle on device vectors b (FP64) and x (FP64, in/out)
-static void vcycle_dev(mgldg_mg* m, const double* b, double* x, bool x_is_zero) {
+// The V-cycle's output s = x_level0 (converted to FP64 in the mixed forms)
+// and the partial sums of b.s, the PCG's r.z, in one pass over the vectors
+// instead of a copy followed by a separate dot product.
+template <class T>
+__global__ void __launch_bounds__(256) k_out_dot(int64_t n, const T* __restrict__ xl, const double* __restrict__ b,
+                                                 double* __restrict__ s, double* __restrict__ partials) {
+    __shared__ double sm[8];
+    double acc = 0;
+    for (int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (int64_t)gridDim.x * 256) {
+        const double v = (double)xl[i];
+        s[i] = v;
+        acc += b[i] * v;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < 8; ++w) t += sm[w];
+        partials[blockIdx.x] = t;
+    }
+}
+
+template <class T>
+static void out_dot(mgldg_ctx* ctx, int64_t n, const T* xl, const double* b, double* s, double* partials) {
+    const int g = reduce_grid((int)std::min<int64_t>(n, 1 << 30));
+    {
+        Launch L(ctx, MGLDG_K_VECTOR);
+        k_out_dot<T><<<g, 256, 0, ctx->stream>>>(n, xl, b, s, partials);
+    }
+    check_launch();
+}
+
+// one V-cycle on device vectors b (FP64) and x (FP64, in/out); with
+// `dot_part`, also the reduce_grid(n) partial sums of b.x of the result
+static void vcycle_dev(mgldg_mg* m, const double* b, double* x, bool x_is_zero, double* dot_part = nullptr) {
     mgldg_ctx* ctx = m->ctx;
     LevelData& L = m->L[0];
     struct LevelReset {
@@ -199,13 +234,15 @@ static void vcycle_dev(mgldg_mg* m, const double* b, double* x, bool x_is_zero) 
         if (x_is_zero) MG_CHECK_CUDA(cudaMemsetAsync(L.x32, 0, L.n * sizeof(float), ctx->stream));
         else convert<double, float>(ctx, L.n, x, L.x32);
         vcycle<float>(m, 0);
-        convert<float, double>(ctx, L.n, L.x32, x);
+        if (dot_part) out_dot<float>(ctx, L.n, L.x32, b, x, dot_part);
+        else convert<float, double>(ctx, L.n, L.x32, x);
     } else {
         MG_CHECK_CUDA(cudaMemcpyAsync(L.bb, b, L.n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
         if (x_is_zero) MG_CHECK_CUDA(cudaMemsetAsync(L.x, 0, L.n * sizeof(double), ctx->stream));
         else MG_CHECK_CUDA(cudaMemcpyAsync(L.x, x, L.n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
         vcycle<double>(m, 0);
-        MG_CHECK_CUDA(cudaMemcpyAsync(x, L.x, L.n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+        if (dot_part) out_dot<double>(ctx, L.n, L.x, b, x, dot_part);
+        else MG_CHECK_CUDA(cudaMemcpyAsync(x, L.x, L.n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
     }
 }
 
@@ -553,7 +590,7 @@ static void ensure_pcg(mgldg_mg* m, mgldg_ctx* ctx, int64_t n, int maxit) {
 
 // Captures one preconditioner application (x = 0, b = r, V-cycle, s = x) as
 // a CUDA graph.  Returns null (and stops trying) if the capture is refused.
-static mgldg_mg::Graph* capture_precon(mgldg_mg* m, const double* r, double* s) {
+static mgldg_mg::Graph* capture_precon(mgldg_mg* m, const double* r, double* s, double* part) {
     mgldg_ctx* ctx = m->ctx;
     mgldg_mg::Graph& g = m->graphs[m->next_graph];
     m->next_graph ^= 1;
@@ -571,7 +608,7 @@ static mgldg_mg::Graph* capture_precon(mgldg_mg* m, const double* r, double* s) 
     }
     bool ok = true;
     try {
-        vcycle_dev(m, r, s, true);
+        vcycle_dev(m, r, s, true, part);
     } catch (...) {
         ok = false;
     }
@@ -593,10 +630,12 @@ static mgldg_mg::Graph* capture_precon(mgldg_mg* m, const double* r, double* s) 
     }
     g.in = r;
     g.out = s;
+    g.part = part;
     return &g;
 }
 
-static void precon(mgldg_mg* m, const double* r, double* s) {
+// s = M(r); with `part`, also the partial sums of r.s (reduce_grid(n) of them)
+static void precon(mgldg_mg* m, const double* r, double* s, double* part = nullptr) {
     mgldg_ctx* ctx = m->ctx;
     if (m->L.empty()) {
         MG_CHECK_CUDA(cudaMemcpyAsync(s, r, m->pcg_n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
@@ -606,18 +645,22 @@ static void precon(mgldg_mg* m, const double* r, double* s) {
     if (!ctx->prof && !m->graphs_off) {
         mgldg_mg::Graph* g = nullptr;
         for (auto& c : m->graphs)
-            if (c.exec && c.in == r && c.out == s) g = &c;
-        if (!g) g = capture_precon(m, r, s);
+            if (c.exec && c.in == r && c.out == s && c.part == part) g = &c;
+        if (!g) g = capture_precon(m, r, s, part);
         if (g) {
             MG_CHECK_CUDA(cudaGraphLaunch(g->exec, ctx->stream));
             for (int k = 0; k < MGLDG_K_NCLASS; ++k) ctx->launches[k] += g->launches[k];
             return;
         }
     }
-    vcycle_dev(m, r, s, true);
+    vcycle_dev(m, r, s, true, part);
 }
 
 void mg_precon(mgldg_mg* m, const double* r, double* s) { precon(m, r, s); }
+void mg_precon_eager(mgldg_mg* m, const double* r, double* s) {
+    if (m->L.empty()) precon(m, r, s);
+    else vcycle_dev(m, r, s, true);
+}
 void mg_take_errors(mgldg_mg* m) { take_errors(m); }
 
 // One PCG iteration (krylov.h:43-61) on the context's stream: q = A d,
@@ -659,10 +702,16 @@ static void pcg_iteration(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const
         k_pcg_rr<<<1, 256, 0, ctx->stream>>>(m->sc, part, np, m->hist, -1);
     }
     check_launch();
-    // s = M(r) ; delta_new = r.s ; beta ; d = s + beta d
-    if (eager && !m->L.empty()) vcycle_dev(m, m->r, m->s, true);
-    else precon(m, m->r, m->s);
-    dot_partials<double>(ctx, (int)n, m->r, m->s, part, &np);
+    // s = M(r) ; delta_new = r.s (summed by the V-cycle's output kernel) ;
+    // beta ; d = s + beta d
+    if (m->L.empty()) {
+        precon(m, m->r, m->s);
+        dot_partials<double>(ctx, (int)n, m->r, m->s, part, &np);
+    } else {
+        if (eager) vcycle_dev(m, m->r, m->s, true, part);
+        else precon(m, m->r, m->s, part);
+        np = reduce_grid((int)std::min<int64_t>(n, 1 << 30));
+    }
     {
         Launch L(ctx, MGLDG_K_VECTOR);
         k_pcg_beta<<<1, 256, 0, ctx->stream>>>(m->sc, part, np);
@@ -768,8 +817,13 @@ static void pcg_dev(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const doubl
     // r = b - A x ; d = M(r) ; delta_new = delta_0 = r.d
     const bool df = df64_ok(m, A) && m->dhi;
     spmv<double>(ctx, A, -1.0, x, 1.0, b, m->r);
-    precon(m, m->r, m->d);
-    dot_partials<double>(ctx, (int)n, m->r, m->d, part, &np);
+    if (m->L.empty()) {
+        precon(m, m->r, m->d);
+        dot_partials<double>(ctx, (int)n, m->r, m->d, part, &np);
+    } else {
+        precon(m, m->r, m->d, part);
+        np = grid_vec;
+    }
     if (df) {
         Launch L(ctx, MGLDG_K_VECTOR);
         k_split<<<grid_vec, 256, 0, ctx->stream>>>(n, m->d, m->dhi, m->dlo);
@@ -786,8 +840,11 @@ static void pcg_dev(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const doubl
     int i = 0;
     bool broke = m->h_sc->breakdown != 0;
     if (broke) maxit = 0;
-    // blocks of iterations as graphs (per-kernel event timing needs eager launches)
-    const bool use_graph = !ctx->prof && !m->pcg_graph_off;
+    // blocks of iterations as graphs (per-kernel event timing needs eager
+    // launches; MGLDG_PCG_HOST_LOOP=1 keeps the host loop for profilers that
+    // cannot see kernels under a conditional graph node)
+    static const bool host_loop = std::getenv("MGLDG_PCG_HOST_LOOP") != nullptr;
+    const bool use_graph = !ctx->prof && !m->pcg_graph_off && !host_loop;
     while (i < maxit && m->h_sc->delta_new > tol2 * m->h_sc->delta0) {
         if (use_graph && !m->pcg_graph_off) {
             mgldg_mg::PcgGraph& G = m->pg;
@@ -845,6 +902,7 @@ mgldg_mg::~mgldg_mg() {
     }
     dfree(Cinv);
     dfree(r); dfree(d); dfree(q); dfree(s); dfree(hist); dfree(dhi); dfree(dlo);
+    dfree(host_b); dfree(host_x);
     dfree(sc);
     if (h_sc) cudaFreeHost(h_sc);
     mg::batch_free(batch);
@@ -922,7 +980,7 @@ extern "C" int mgldg_mg_create(mgldg_ctx* ctx, const mgldg_ops* fine, const mgld
     MG_REQUIRE(p.restriction == MGLDG_RESTRICT_RAT || p.restriction == MGLDG_RESTRICT_RATRAT, MGLDG_ERR_ARG,
                "Unknown restriction method.");
     MG_REQUIRE(p.precision == MGLDG_PREC_FP64 || p.precision == MGLDG_PREC_MIXED ||
-                   p.precision == MGLDG_PREC_MIXED_F16,
+                   p.precision == MGLDG_PREC_MIXED_F16 || p.precision == MGLDG_PREC_MIXED_TF32,
                MGLDG_ERR_ARG, "Unknown precision.");
     MG_REQUIRE(p.npre >= 0 && p.npost >= 0, MGLDG_ERR_ARG, "negative smoothing count");
     MG_REQUIRE(fine->A != nullptr, MGLDG_ERR_ARG, "fine operators lack A (call construct_laplacian)");
@@ -962,6 +1020,11 @@ extern "C" int mgldg_mg_create(mgldg_ctx* ctx, const mgldg_ops* fine, const mgld
             m->L[i + 1].ops = c;
             m->L[i + 1].owns_ops = true;
             phase("galerkin", i);
+            if (trace) {
+                double pl = 0, pr = 0;
+                setup_clock_take(&pl, &pr);
+                std::fprintf(stderr, "[mgldg setup] level %d   host plans %.1f ms, GPU products %.1f ms\n", i, pl, pr);
+            }
             if (p.precision != MGLDG_PREC_FP64) {
                 bsr_ensure_fp32(Tc);
                 bsr_ensure_fp32(m->L[i].Tt);
@@ -1101,15 +1164,31 @@ extern "C" int mgldg_pcg(mgldg_ctx* ctx, mgldg_mg* m, const mgldg_bsr* A, const 
     MG_REQUIRE(A->br == A->bc && A->nbr == A->nbc, MGLDG_ERR_SHAPE, "pcg needs a square matrix");
     if (m) MG_REQUIRE(m->L[0].n == (int64_t)A->nbr * A->br, MGLDG_ERR_SHAPE, "preconditioner size mismatch");
     const int64_t n = (int64_t)A->nbr * A->br;
+    if (m) {
+        // the multigrid object keeps the device copies between calls
+        if (m->host_n != n) {
+            dfree(m->host_b);
+            dfree(m->host_x);
+            m->host_b = m->host_x = nullptr;
+            m->host_n = 0;
+            m->host_b = dalloc<double>(n);
+            m->host_x = dalloc<double>(n);
+            m->host_n = n;
+        }
+        upload(ctx, m->host_b, b, n);
+        upload(ctx, m->host_x, x, n);
+        pcg_dev(ctx, m, A, m->host_b, m->host_x, tol, maxit, iters, res_hist);
+        download(ctx, x, m->host_x, n);
+        sync(ctx);
+        return MGLDG_OK;
+    }
     double *db = nullptr, *dx = nullptr;
     try {
         db = dalloc<double>(n);
         dx = dalloc<double>(n);
         upload(ctx, db, b, n);
         upload(ctx, dx, x, n);
-        if (m) {
-            pcg_dev(ctx, m, A, db, dx, tol, maxit, iters, res_hist);
-        } else {
+        {
             mgldg_mg plain;
             plain.ctx = ctx;
             mgldg_mg_params_default(&plain.p);

@@ -49,6 +49,8 @@ void seg_free(SegWork* w);
 // one preconditioner application s = V-cycle(r) from x = 0 (graph replay
 // when possible) and the collection of device-side error reports (mg.cu)
 void mg_precon(mgldg_mg* m, const double* r, double* s);
+// the same with every launch issued directly (for capture into a graph)
+void mg_precon_eager(mgldg_mg* m, const double* r, double* s);
 void mg_take_errors(mgldg_mg* m);
 
 struct PcgScalars {
@@ -77,6 +79,7 @@ struct mgldg_mg {
     struct Graph {
         const double* in = nullptr;
         double* out = nullptr;
+        double* part = nullptr;   // r.s partial sums written by the graph (or none)
         cudaGraphExec_t exec = nullptr;
         int64_t launches[MGLDG_K_NCLASS] = {0};
     };
@@ -98,6 +101,10 @@ struct mgldg_mg {
     };
     PcgGraph pg;
     bool pcg_graph_off = false;
+    // device copies of the host vectors of mgldg_pcg, kept between calls
+    // (stable addresses let the iteration graph be reused)
+    double *host_b = nullptr, *host_x = nullptr;
+    int64_t host_n = 0;
     mg::Batch* batch = nullptr;   // multi-RHS work space (batched.cu)
     mg::SegWork* seg = nullptr;   // segmented-PCG work space (batched.cu)
     ~mgldg_mg();

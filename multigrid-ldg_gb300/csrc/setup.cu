@@ -13,6 +13,7 @@
 // sum over terms runs in a fixed order (the reference's order over d and k),
 // and every output block is computed by exactly one CTA.
 #include <algorithm>
+#include <chrono>
 #include <numeric>
 
 #include "api.cuh"
@@ -20,6 +21,21 @@
 using namespace mg;
 
 namespace mg {
+
+// setup phase clocks (host symbolic plans, GPU numeric products), read by
+// the MGLDG_SETUP_TRACE report of mgldg_mg_create
+static double g_plan_ms = 0, g_prod_ms = 0;
+void setup_clock_take(double* plan_ms, double* prod_ms) {
+    *plan_ms = g_plan_ms;
+    *prod_ms = g_prod_ms;
+    g_plan_ms = g_prod_ms = 0;
+}
+struct Clock {
+    double* acc;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    explicit Clock(double* a) : acc(a) {}
+    ~Clock() { *acc += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(); }
+};
 
 struct Term {
     int x, m, y;
@@ -104,6 +120,7 @@ static void expand_plan(Plan& P, const Plan& U) {
 
 // C = op(X) * Y   (multiply_mm when !tX, multiply_mm_t when tX)
 static Plan plan_mm(const mgldg_bsr* X, bool tX, const mgldg_bsr* Y) {
+    Clock clk(&g_plan_ms);
     Plan P;
     std::vector<KeyTerm> kt;
     if (!tX) {
@@ -145,6 +162,7 @@ static Plan plan_mm(const mgldg_bsr* X, bool tX, const mgldg_bsr* Y) {
 // coarse mass matrix.  `extra` adds output keys (the T pattern).
 static Plan plan_triple(const std::vector<const mgldg_bsr*>& Xs, const mgldg_bsr* D, const mgldg_bsr* extra,
                         std::vector<Plan>* per_dim) {
+    Clock clk(&g_plan_ms);
     const mgldg_bsr* X0 = Xs[0];
     int nout = X0->nbc;
     per_dim->clear();
@@ -261,6 +279,7 @@ static void run_plan(mgldg_ctx* ctx, const Plan& P, int oR, int oC, Opnd X, bool
                      const double* init, double* out) {
     int nout = (int)P.col_idx.size();
     if (nout == 0) return;
+    Clock clk(&g_prod_ms);
     MG_REQUIRE(oR * oC <= 1024 && X.r * X.c <= 1024 && Y.r * Y.c <= 1024 && Mm.r * Mm.c <= 1024,
                MGLDG_ERR_UNSUPPORTED, "block products limited to 32x32 blocks");
     int* dptr = nullptr;

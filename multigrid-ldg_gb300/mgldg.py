@@ -20,7 +20,7 @@ OK, ERR_ARG, ERR_SHAPE, ERR_CUDA, ERR_BREAKDOWN, ERR_TIMEOUT, ERR_NOT_SPD, ERR_N
 RELAX_JACOBI, RELAX_GAUSS_SEIDEL = 0, 1
 COARSE_CHOLESKY, COARSE_RELAXATION, COARSE_DENSE = 0, 1, 2
 RESTRICT_RAT, RESTRICT_RATRAT = 0, 1
-PREC_FP64, PREC_MIXED, PREC_MIXED_F16 = 0, 1, 2
+PREC_FP64, PREC_MIXED, PREC_MIXED_F16, PREC_MIXED_TF32 = 0, 1, 2, 3
 K_SPMV, K_GS, K_JACOBI, K_TRANSFER, K_COARSE, K_VECTOR, K_SETUP = range(7)
 K_NAMES = ["spmv", "gauss_seidel", "jacobi", "transfer", "coarse", "vector", "setup"]
 

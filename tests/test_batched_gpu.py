@@ -127,6 +127,41 @@ def test_batched_mixed_matches_single_rhs(ctx):
     assert all(t in (32, 64, 128) for t in tiles)
 
 
+@pytest.mark.parametrize("P,n,k", [(3, 32, 64), (4, 16, 20), (3, 16, 130)])
+def test_batched_tensor_core_form(ctx, P, n, k):
+    # MGLDG_PREC_MIXED_TF32: the multi-RHS V-cycle's level products on the
+    # tensor cores (3xTF32 split products, FP32 accumulation).  One V-cycle
+    # must match the FP32 CUDA-core V-cycle to FP32 rounding, and the block
+    # PCG must reach the FP64 solution of every column within 1e-10 in about
+    # as many iterations; block sizes 9 (Q2) and 16 (Q3), 64-column tiles
+    # full, partial (20) and over two tiles (130)
+    torch = pytest.importorskip("torch")
+    prob = mgldg.CartesianProblem(ctx, P, n)
+    kw = dict(relaxation=mgldg.RELAX_JACOBI, omega=0.7, npre=2, npost=2, solver=mgldg.COARSE_DENSE,
+              max_levels=4, mean_project=0)
+    mg32 = mgldg.Multigrid(ctx, prob.ops, prob.T, precision=mgldg.PREC_MIXED, **kw)
+    mgtc = mgldg.Multigrid(ctx, prob.ops, prob.T, precision=mgldg.PREC_MIXED_TF32, **kw)
+    rng = np.random.default_rng(k)
+    Bv = rng.standard_normal((prob.ndof, k))
+    outs = []
+    for mg in (mg32, mgtc):
+        dB, dX = _dev(torch, Bv), _dev(torch, np.zeros_like(Bv))
+        torch.cuda.synchronize()
+        ctx.check(mgldg.lib().mgldg_mg_vcycle_batched_dev(ctx.h, mg.h, k, C.c_void_p(dB.data_ptr()),
+                                                          C.c_void_p(dX.data_ptr())), "vcycle_batched")
+        ctx.sync()
+        outs.append(dX.cpu().numpy())
+    assert np.abs(outs[1] - outs[0]).max() <= 1e-5 * np.abs(outs[0]).max()
+    B = np.stack([prob.rhs_gaussian(3000 + c) for c in range(k)], axis=1)
+    X32, its32, _ = mgldg.pcg_batched(ctx, prob.ops.A, B, precon=mg32, tol=1e-11, maxit=200)
+    Xtc, itstc, _ = mgldg.pcg_batched(ctx, prob.ops.A, B, precon=mgtc, tol=1e-11, maxit=200)
+    assert np.all(np.abs(itstc - its32) <= 2)
+    fp64 = mgldg.Multigrid(ctx, prob.ops, prob.T, **kw)
+    for c in (0, k // 2, k - 1):
+        xd, _ = mgldg.pcg(ctx, prob.ops.A, B[:, c], precon=fp64, tol=1e-13)
+        assert np.linalg.norm(Xtc[:, c] - xd) <= 1e-10 * np.linalg.norm(xd)
+
+
 def test_frozen_and_zero_columns(ctx):
     P, n = 3, 16
     prob = mgldg.CartesianProblem(ctx, P, n)
