@@ -312,57 +312,103 @@ __device__ __forceinline__ void mma_3xtf32(float (&d)[4], const unsigned (&ah)[4
     mma_tf32(d, ah, bh);
 }
 
-// A operand rows g, g+8, columns ka = 8 s + t and ka + 4 of a b x b row-major block
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// per-warp shared-memory stages of k_spmm_mma: the b x b block (16 x AS,
+// zero beyond b) and the block's 16 x 64 slice of X (rows beyond b zero),
+// twice (double buffering)
+constexpr int kMmaWarps = 4;
+constexpr int kMmaXS = 72;   // X row stride: conflict-free B-operand reads
+constexpr int kMmaAS = 20;   // A row stride: conflict-free A-operand reads
+struct MmaStage {
+    float x[2][16 * kMmaXS];
+    float a[2][16 * kMmaAS];
+};
+
+// issues the copies of block kk (its values and its X slice) into stage buf
 template <int B>
-__device__ __forceinline__ void a_frag(const float* __restrict__ A, int s, int g, int t, unsigned (&ah)[4],
-                                       unsigned (&al)[4]) {
-    const int ka = s * 8 + t, kb = ka + 4;
+__device__ __forceinline__ void mma_prefetch(const SpmmArgs<float>& a, int kk, int c0, MmaStage& st, int buf,
+                                             int lane) {
+    const float* A = a.val + (size_t)(a.blk ? a.blk[kk] : kk) * (B * B);
+    for (int q = lane; q < B * B; q += 32) cp_async4(&st.a[buf][(q / B) * kMmaAS + q % B], A + q);
+    const float* xb = a.X + (size_t)a.col_idx[kk] * B * a.k + c0;
+    const int ncols = min(64, a.k - c0);   // a multiple of 4
+    for (int q = lane; q < B * 16; q += 32) {
+        const int r = q >> 4, c4 = (q & 15) * 4;
+        if (c4 < ncols) cp_async16(&st.x[buf][r * kMmaXS + c4], xb + (size_t)r * a.k + c4);
+    }
+}
+
+// A operand (rows g, g+8; columns 8 s + t, + 4) from a staged 16 x AS block
+__device__ __forceinline__ void a_frag_s(const float* As, int s, int g, int t, unsigned (&ah)[4], unsigned (&al)[4]) {
+    const int ka = s * 8 + t;
     float v[4];
-    v[0] = (g < B && ka < B) ? __ldg(A + g * B + ka) : 0.f;
-    v[1] = (g + 8 < B && ka < B) ? __ldg(A + (g + 8) * B + ka) : 0.f;
-    v[2] = (g < B && kb < B) ? __ldg(A + g * B + kb) : 0.f;
-    v[3] = (g + 8 < B && kb < B) ? __ldg(A + (g + 8) * B + kb) : 0.f;
+    v[0] = As[g * kMmaAS + ka];
+    v[1] = As[(g + 8) * kMmaAS + ka];
+    v[2] = As[g * kMmaAS + ka + 4];
+    v[3] = As[(g + 8) * kMmaAS + ka + 4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) split_tf32(v[q], ah[q], al[q]);
 }
 
 template <int B, int MODE>
-__global__ void __launch_bounds__(256) k_spmm_mma(const SpmmArgs<float> a) {
+__global__ void __launch_bounds__(kMmaWarps * 32) k_spmm_mma(const SpmmArgs<float> a) {
     static_assert(B >= 1 && B <= 16, "tensor-core SpMM takes blocks up to 16 x 16");
     constexpr int KS = (B + 7) / 8;   // k-steps of 8
-    constexpr int RS = 72;            // row stride of the staged Jacobi tile (conflict-free B reads)
-    __shared__ float tile[8][16 * RS];
+    __shared__ __align__(16) MmaStage stages[kMmaWarps];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int g = lane >> 2, t = lane & 3;
     const int k = a.k;
     const int c0 = blockIdx.y * 64;
-    for (int i = blockIdx.x * 8 + warp; i < a.nbr; i += gridDim.x * 8) {
+    MmaStage& st = stages[warp];
+    // zero both stages once: rows and columns beyond b stay zero (finite)
+    for (int q = lane; q < 2 * 16 * kMmaXS; q += 32) (&st.x[0][0])[q] = 0.f;
+    for (int q = lane; q < 2 * 16 * kMmaAS; q += 32) (&st.a[0][0])[q] = 0.f;
+    __syncwarp();
+    for (int i = blockIdx.x * kMmaWarps + warp; i < a.nbr; i += gridDim.x * kMmaWarps) {
         float acc[8][4];
 #pragma unroll
         for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
             for (int q = 0; q < 4; ++q) acc[nt][q] = 0.f;
         const int k0 = a.row_ptr[i], k1 = a.row_ptr[i + 1];
+        if (k0 < k1) mma_prefetch<B>(a, k0, c0, st, 0, lane);
+        cp_async_commit();
         for (int kk = k0; kk < k1; ++kk) {
-            const float* A = a.val + (size_t)(a.blk ? a.blk[kk] : kk) * (B * B);
-            const float* xb = a.X + (size_t)a.col_idx[kk] * B * k;
+            const int buf = (kk - k0) & 1;
+            if (kk + 1 < k1) mma_prefetch<B>(a, kk + 1, c0, st, buf ^ 1, lane);
+            cp_async_commit();
+            cp_async_wait<1>();   // block kk has landed (kk + 1 may be in flight)
+            __syncwarp();
+            const float* As = st.a[buf];
+            const float* Xs = st.x[buf];
 #pragma unroll
             for (int s = 0; s < KS; ++s) {
                 unsigned ah[4], al[4];
-                a_frag<B>(A, s, g, t, ah, al);
-                const int ka = s * 8 + t, kb = ka + 4;
+                a_frag_s(As, s, g, t, ah, al);
+                const int ka = s * 8 + t;
 #pragma unroll
                 for (int nt = 0; nt < 8; ++nt) {
-                    const int col = c0 + nt * 8 + g;
-                    const float x0 = (ka < B && col < k) ? __ldg(xb + (size_t)ka * k + col) : 0.f;
-                    const float x1 = (kb < B && col < k) ? __ldg(xb + (size_t)kb * k + col) : 0.f;
                     unsigned bh[2], bl[2];
-                    split_tf32(x0, bh[0], bl[0]);
-                    split_tf32(x1, bh[1], bl[1]);
+                    split_tf32(Xs[ka * kMmaXS + nt * 8 + g], bh[0], bl[0]);
+                    split_tf32(Xs[(ka + 4) * kMmaXS + nt * 8 + g], bh[1], bl[1]);
                     mma_3xtf32(acc[nt], ah, al, bh, bl);
                 }
             }
+            __syncwarp();   // stage buf is rewritten by the prefetch two blocks on
         }
+        cp_async_wait<0>();
+        __syncwarp();
         const size_t y0 = (size_t)i * B * k;
         if constexpr (MODE == 0) {
 #pragma unroll
@@ -380,8 +426,12 @@ __global__ void __launch_bounds__(256) k_spmm_mma(const SpmmArgs<float> a) {
                         }
                     }
         } else {
-            // t = B_i - (A X)_i into the warp's tile (rows >= b are zero)
-            float* T = tile[warp];
+            // t = B_i - (A X)_i into stage 0's X slice (rows beyond b stay
+            // zero), Dinv_i into stage 0's block, then Y_i = X_i + omega Dinv_i t
+            float* T = st.x[0];
+            float* Ds = st.a[0];
+            const float* D = a.Dinv + (size_t)i * B * B;
+            for (int q = lane; q < B * B; q += 32) Ds[(q / B) * kMmaAS + q % B] = __ldg(D + q);
 #pragma unroll
             for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
@@ -389,28 +439,24 @@ __global__ void __launch_bounds__(256) k_spmm_mma(const SpmmArgs<float> a) {
 #pragma unroll
                     for (int e = 0; e < 2; ++e) {
                         const int row = g + 8 * h, cl = nt * 8 + 2 * t + e, col = c0 + cl;
-                        float v = 0.f;
-                        if (row < B && col < k) v = a.B[y0 + (size_t)row * k + col] - acc[nt][2 * h + e];
-                        T[row * RS + cl] = v;
+                        if (row < B) T[row * kMmaXS + cl] = (col < k) ? a.B[y0 + (size_t)row * k + col] - acc[nt][2 * h + e] : 0.f;
                     }
             __syncwarp();
-            float out[8][4];
 #pragma unroll
             for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
-                for (int q = 0; q < 4; ++q) out[nt][q] = 0.f;
-            const float* D = a.Dinv + (size_t)i * B * B;
+                for (int q = 0; q < 4; ++q) acc[nt][q] = 0.f;
 #pragma unroll
             for (int s = 0; s < KS; ++s) {
                 unsigned ah[4], al[4];
-                a_frag<B>(D, s, g, t, ah, al);
-                const int ka = s * 8 + t, kb = ka + 4;
+                a_frag_s(Ds, s, g, t, ah, al);
+                const int ka = s * 8 + t;
 #pragma unroll
                 for (int nt = 0; nt < 8; ++nt) {
                     unsigned bh[2], bl[2];
-                    split_tf32(T[ka * RS + nt * 8 + g], bh[0], bl[0]);
-                    split_tf32(T[kb * RS + nt * 8 + g], bh[1], bl[1]);
-                    mma_3xtf32(out[nt], ah, al, bh, bl);
+                    split_tf32(T[ka * kMmaXS + nt * 8 + g], bh[0], bl[0]);
+                    split_tf32(T[(ka + 4) * kMmaXS + nt * 8 + g], bh[1], bl[1]);
+                    mma_3xtf32(acc[nt], ah, al, bh, bl);
                 }
             }
             __syncwarp();
@@ -423,7 +469,7 @@ __global__ void __launch_bounds__(256) k_spmm_mma(const SpmmArgs<float> a) {
                         const int row = g + 8 * h, col = c0 + nt * 8 + 2 * t + e;
                         if (row < B && col < k) {
                             const size_t idx = y0 + (size_t)row * k + col;
-                            a.Y[idx] = a.X[idx] + a.omega * out[nt][2 * h + e];
+                            a.Y[idx] = a.X[idx] + a.omega * acc[nt][2 * h + e];
                         }
                     }
         }
@@ -436,13 +482,13 @@ template <int B, int MODE>
 static void launch_mma(mgldg_ctx* ctx, const SpmmArgs<float>& a, int kclass) {
     const int ncolt = (a.k + 63) / 64;
     int per_sm = 0;
-    MG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spmm_mma<B, MODE>, 256, 0));
+    MG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spmm_mma<B, MODE>, kMmaWarps * 32, 0));
     per_sm = std::max(1, per_sm);
-    const int want = (a.nbr + 7) / 8;
+    const int want = (a.nbr + kMmaWarps - 1) / kMmaWarps;
     const int gx = std::max(1, std::min(want, ctx->sm_count * per_sm * 4 / std::max(1, ncolt) + 1));
     {
         Launch L(ctx, kclass);
-        k_spmm_mma<B, MODE><<<dim3(gx, ncolt), 256, 0, ctx->stream>>>(a);
+        k_spmm_mma<B, MODE><<<dim3(gx, ncolt), kMmaWarps * 32, 0, ctx->stream>>>(a);
     }
     check_launch();
 }
@@ -510,7 +556,7 @@ template <class T>
 static void spmm_launch(mgldg_ctx* ctx, int br, int bc, const SpmmArgs<T>& a, int mode, TileCfg cfg, int kclass) {
     if (a.nbr == 0 || a.k == 0) return;
     if constexpr (sizeof(T) == 4) {
-        if (cfg.mma && mma_shape(br, bc)) {
+        if (cfg.mma && mma_shape(br, bc) && a.k % 4 == 0 && aligned(a.X, 16)) {
             spmm_mma(ctx, br, a, mode, kclass);
             return;
         }
