@@ -350,6 +350,7 @@ __device__ __forceinline__ void mma_prefetch(const SpmmArgs<float>& a, int kk, i
 }
 
 // A operand (rows g, g+8; columns 8 s + t, + 4) from a staged 16 x AS block
+template <bool SPLIT>
 __device__ __forceinline__ void a_frag_s(const float* As, int s, int g, int t, unsigned (&ah)[4], unsigned (&al)[4]) {
     const int ka = s * 8 + t;
     float v[4];
@@ -358,10 +359,29 @@ __device__ __forceinline__ void a_frag_s(const float* As, int s, int g, int t, u
     v[2] = As[g * kMmaAS + ka + 4];
     v[3] = As[(g + 8) * kMmaAS + ka + 4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) split_tf32(v[q], ah[q], al[q]);
+    for (int q = 0; q < 4; ++q) {
+        if constexpr (SPLIT) split_tf32(v[q], ah[q], al[q]);
+        else ah[q] = f2tf32(v[q]);
+    }
 }
 
-template <int B, int MODE>
+// one k-step x n-tile product: split (3xTF32) or plain TF32
+template <bool SPLIT>
+__device__ __forceinline__ void mma_step(float (&d)[4], const unsigned (&ah)[4], const unsigned (&al)[4], float x0,
+                                         float x1) {
+    unsigned bh[2], bl[2];
+    if constexpr (SPLIT) {
+        split_tf32(x0, bh[0], bl[0]);
+        split_tf32(x1, bh[1], bl[1]);
+        mma_3xtf32(d, ah, al, bh, bl);
+    } else {
+        bh[0] = f2tf32(x0);
+        bh[1] = f2tf32(x1);
+        mma_tf32(d, ah, bh);
+    }
+}
+
+template <int B, int MODE, bool SPLIT>
 __global__ void __launch_bounds__(kMmaWarps * 32) k_spmm_mma(const SpmmArgs<float> a) {
     static_assert(B >= 1 && B <= 16, "tensor-core SpMM takes blocks up to 16 x 16");
     constexpr int KS = (B + 7) / 8;   // k-steps of 8
@@ -395,15 +415,11 @@ __global__ void __launch_bounds__(kMmaWarps * 32) k_spmm_mma(const SpmmArgs<floa
 #pragma unroll
             for (int s = 0; s < KS; ++s) {
                 unsigned ah[4], al[4];
-                a_frag_s(As, s, g, t, ah, al);
+                a_frag_s<SPLIT>(As, s, g, t, ah, al);
                 const int ka = s * 8 + t;
 #pragma unroll
-                for (int nt = 0; nt < 8; ++nt) {
-                    unsigned bh[2], bl[2];
-                    split_tf32(Xs[ka * kMmaXS + nt * 8 + g], bh[0], bl[0]);
-                    split_tf32(Xs[(ka + 4) * kMmaXS + nt * 8 + g], bh[1], bl[1]);
-                    mma_3xtf32(acc[nt], ah, al, bh, bl);
-                }
+                for (int nt = 0; nt < 8; ++nt)
+                    mma_step<SPLIT>(acc[nt], ah, al, Xs[ka * kMmaXS + nt * 8 + g], Xs[(ka + 4) * kMmaXS + nt * 8 + g]);
             }
             __syncwarp();   // stage buf is rewritten by the prefetch two blocks on
         }
@@ -449,15 +465,11 @@ __global__ void __launch_bounds__(kMmaWarps * 32) k_spmm_mma(const SpmmArgs<floa
 #pragma unroll
             for (int s = 0; s < KS; ++s) {
                 unsigned ah[4], al[4];
-                a_frag_s(Ds, s, g, t, ah, al);
+                a_frag_s<SPLIT>(Ds, s, g, t, ah, al);
                 const int ka = s * 8 + t;
 #pragma unroll
-                for (int nt = 0; nt < 8; ++nt) {
-                    unsigned bh[2], bl[2];
-                    split_tf32(T[ka * kMmaXS + nt * 8 + g], bh[0], bl[0]);
-                    split_tf32(T[(ka + 4) * kMmaXS + nt * 8 + g], bh[1], bl[1]);
-                    mma_3xtf32(acc[nt], ah, al, bh, bl);
-                }
+                for (int nt = 0; nt < 8; ++nt)
+                    mma_step<SPLIT>(acc[nt], ah, al, T[ka * kMmaXS + nt * 8 + g], T[(ka + 4) * kMmaXS + nt * 8 + g]);
             }
             __syncwarp();
 #pragma unroll
@@ -478,19 +490,27 @@ __global__ void __launch_bounds__(kMmaWarps * 32) k_spmm_mma(const SpmmArgs<floa
 
 static bool mma_shape(int br, int bc) { return br == bc && (br == 4 || br == 6 || br == 9 || br == 10 || br == 16); }
 
-template <int B, int MODE>
-static void launch_mma(mgldg_ctx* ctx, const SpmmArgs<float>& a, int kclass) {
+template <int B, int MODE, bool SPLIT>
+static void launch_mma_t(mgldg_ctx* ctx, const SpmmArgs<float>& a, int kclass) {
     const int ncolt = (a.k + 63) / 64;
     int per_sm = 0;
-    MG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spmm_mma<B, MODE>, kMmaWarps * 32, 0));
+    MG_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spmm_mma<B, MODE, SPLIT>, kMmaWarps * 32, 0));
     per_sm = std::max(1, per_sm);
     const int want = (a.nbr + kMmaWarps - 1) / kMmaWarps;
     const int gx = std::max(1, std::min(want, ctx->sm_count * per_sm * 4 / std::max(1, ncolt) + 1));
     {
         Launch L(ctx, kclass);
-        k_spmm_mma<B, MODE><<<dim3(gx, ncolt), kMmaWarps * 32, 0, ctx->stream>>>(a);
+        k_spmm_mma<B, MODE, SPLIT><<<dim3(gx, ncolt), kMmaWarps * 32, 0, ctx->stream>>>(a);
     }
     check_launch();
+}
+
+// (the plain-TF32 instantiation, SPLIT = false, measured slower per sweep
+// than the CUDA-core kernel as well and needed 10-30% more iterations; the
+// form uses the split products)
+template <int B, int MODE>
+static void launch_mma(mgldg_ctx* ctx, const SpmmArgs<float>& a, int kclass) {
+    launch_mma_t<B, MODE, true>(ctx, a, kclass);
 }
 
 static void spmm_mma(mgldg_ctx* ctx, int b, const SpmmArgs<float>& a, int mode, int kclass) {
