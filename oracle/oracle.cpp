@@ -930,6 +930,11 @@ struct Problem {
     bool simplex = false;
     int s_ne = 0, s_nf = 0, s_nb = 0;
     std::vector<std::vector<int>> agg;   // per agglomeration level: aggregate of each finer element
+    struct AggQuality {
+        int n;
+        double mean_ratio, max_ratio;
+    };
+    std::vector<AggQuality> agg_quality;   // per agglomeration level
     std::vector<double> s_xy;            // node coordinates (s_dim per DOF) in DOF order
     int s_dim = 2;
 };

@@ -83,6 +83,20 @@ int orc_simplex_master_nd(int N, int P, double* mass, double* diff, double* node
 /* block shape of hierarchy level l; aggregate of every finer element at agglomeration level l */
 int orc_hier_block(const orc_problem* pr, int l, int* br, int* bc);
 int orc_problem_partition(const orc_problem* pr, int l, int* agg);
+/* External agglomerator for the simplex hierarchies created after this call
+ * (null restores the greedy seeded one).  It receives one level's weighted
+ * dual graph in CSR form -- n nodes, xadj[n+1], adjncy / adjwgt (shared face
+ * measure), vvol (node volume), vsurf (boundary face measure) -- and the
+ * dimension N, writes part[n] and returns the number of aggregates (the
+ * argument list of MGridGen, lib/ParMGridGen-1.0/mgridgen.h, as the
+ * reference's src/unstructured/mesh/agglomeration.h:53-225 fills it). */
+typedef int (*orc_agglomerator)(int n, const int* xadj, const int* adjncy, const double* adjwgt,
+                                const double* vvol, const double* vsurf, int N, int* part);
+int orc_set_agglomerator(orc_agglomerator fn);
+/* Shape of agglomeration level l's aggregates: count, mean and largest
+ * isoperimetric ratio (2-D: S^2 / (4 pi V), 3-D: S^3 / (36 pi V^2), S the
+ * aggregate's surface, V its volume; 1 for a disk / ball). */
+int orc_problem_agg_quality(const orc_problem* pr, int l, int* naggs, double* mean_ratio, double* max_ratio);
 /* simplex master element (N = 1 or 2): mass, diff matrices (row-major npl x npl), nodes[npl*N] */
 int orc_simplex_master(int N, int P, double* mass, double* diff0, double* diff1, double* nodes);
 int orc_problem_destroy(orc_problem* pr);

@@ -25,6 +25,9 @@ OP_M, OP_G0, OP_G1, OP_T, OP_A, OP_G2 = 0, 1, 2, 3, 4, 5
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_cip, _cdp = C.POINTER(C.c_int), C.POINTER(C.c_double)
+# external agglomerator of the simplex hierarchies (oracle.h orc_agglomerator)
+AGGLOMERATOR = C.CFUNCTYPE(C.c_int, C.c_int, _cip, _cip, _cdp, _cdp, _cdp, C.c_int, _cip)
 
 
 def build():
@@ -90,8 +93,35 @@ def lib():
         L.orc_simplex_problem_create_nd.argtypes = [C.c_int, C.c_int, _dp, C.c_int, _ip, C.c_int, C.c_double,
                                                     C.c_double, C.c_int, C.c_uint64, C.c_uint64, pvp]
         L.orc_simplex_master_nd.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp]
+        L.orc_set_agglomerator.argtypes = [AGGLOMERATOR]
+        L.orc_problem_agg_quality.argtypes = [vp, C.c_int, _cip, _cdp, _cdp]
         _lib = L
     return _lib
+
+
+def set_agglomerator(fn):
+    """Python callable fn(n, xadj, adjncy, adjwgt, vvol, vsurf, N, part) -> count
+    (numpy views of the level's dual graph; fills part) used by the simplex
+    hierarchies created until the next call; None restores the greedy one.
+    Returns the ctypes callback, which the caller keeps alive meanwhile."""
+    if fn is None:
+        lib().orc_set_agglomerator(AGGLOMERATOR())
+        return None
+
+    def tramp(n, xadj, adjncy, adjwgt, vvol, vsurf, N, part):
+        try:
+            xa = np.ctypeslib.as_array(xadj, (n + 1,))
+            m = int(xa[n])
+            views = (xa, np.ctypeslib.as_array(adjncy, (max(m, 1),))[:m],
+                     np.ctypeslib.as_array(adjwgt, (max(m, 1),))[:m], np.ctypeslib.as_array(vvol, (n,)),
+                     np.ctypeslib.as_array(vsurf, (n,)))
+            return int(fn(n, *views, N, np.ctypeslib.as_array(part, (n,))))
+        except Exception:
+            return -1
+
+    cb = AGGLOMERATOR(tramp)
+    lib().orc_set_agglomerator(cb)
+    return cb
 
 
 def _ck(rc, what):
@@ -237,6 +267,12 @@ class Problem:
         agg = np.zeros(sizes[l], np.int32)
         _ck(lib().orc_problem_partition(self.h, l, agg), "partition")
         return agg
+
+    def agg_quality(self, l):
+        """(aggregates, mean and largest isoperimetric ratio) of agglomeration level l."""
+        n, mean, mx = C.c_int(), C.c_double(), C.c_double()
+        _ck(lib().orc_problem_agg_quality(self.h, l, C.byref(n), C.byref(mean), C.byref(mx)), "agg_quality")
+        return n.value, mean.value, mx.value
 
     def _attach(self, h, P):
         self.h = h
