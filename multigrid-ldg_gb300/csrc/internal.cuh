@@ -244,7 +244,7 @@ void construct_laplacian(mgldg_ctx* ctx, mgldg_ops* ops);
 mgldg_bsr* laplacian_of(mgldg_ctx* ctx, mgldg_bsr* M, mgldg_bsr* const* G, int ndim, mgldg_bsr* T);
 void block_inverse(mgldg_ctx* ctx, const mgldg_bsr* A, double* out, int* status);
 mgldg_ops* galerkin_ratrat(mgldg_ctx* ctx, const mgldg_ops* f, const mgldg_bsr* T);
-// host-plan and GPU-product milliseconds of the Galerkin products since the
+// symbolic-plan and numeric-product milliseconds of the Galerkin products since the
 // last call (setup tracing)
 void setup_clock_take(double* plan_ms, double* prod_ms);
 mgldg_ops* galerkin_rat(mgldg_ctx* ctx, const mgldg_ops* f, const mgldg_bsr* T);

@@ -1023,7 +1023,7 @@ extern "C" int mgldg_mg_create(mgldg_ctx* ctx, const mgldg_ops* fine, const mgld
             if (trace) {
                 double pl = 0, pr = 0;
                 setup_clock_take(&pl, &pr);
-                std::fprintf(stderr, "[mgldg setup] level %d   host plans %.1f ms, GPU products %.1f ms\n", i, pl, pr);
+                std::fprintf(stderr, "[mgldg setup] level %d   symbolic plans %.1f ms, numeric products %.1f ms\n", i, pl, pr);
             }
             if (p.precision != MGLDG_PREC_FP64) {
                 bsr_ensure_fp32(Tc);

@@ -1,6 +1,6 @@
-// setup.cu -- Galerkin coarsening setup: block SpGEMM (symbolic on the host,
-// numeric on the GPU), batched block inverses, the Laplacian triple product
-// and the dense inverse of the coarsest level.
+// setup.cu -- Galerkin coarsening setup: block SpGEMM (symbolic pass in
+// plan.cu, numeric pass here, both on the GPU), batched block inverses, the
+// Laplacian triple product and the dense inverse of the coarsest level.
 //
 // Follows the reference's Level coarse constructor
 // (src/cartesian/multigrid/multigrid.h:105-171), construct_laplacian
@@ -17,12 +17,13 @@
 #include <numeric>
 
 #include "api.cuh"
+#include "plan.cuh"
 
 using namespace mg;
 
 namespace mg {
 
-// setup phase clocks (host symbolic plans, GPU numeric products), read by
+// setup phase clocks (symbolic plans, numeric products), read by
 // the MGLDG_SETUP_TRACE report of mgldg_mg_create
 static double g_plan_ms = 0, g_prod_ms = 0;
 void setup_clock_take(double* plan_ms, double* prod_ms) {
@@ -36,174 +37,6 @@ struct Clock {
     explicit Clock(double* a) : acc(a) {}
     ~Clock() { *acc += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(); }
 };
-
-struct Term {
-    int x, m, y;
-};
-
-// output pattern + ordered terms per output block
-struct Plan {
-    int nbr = 0, nbc = 0;
-    std::vector<int> row_ptr, col_idx;
-    std::vector<int> tptr;
-    std::vector<Term> terms;
-};
-
-struct KeyTerm {
-    int64_t key;
-    Term t;
-};
-
-// Orders the terms by output block and builds the output pattern.  Terms go
-// to their output row by a stable counting sort, then each row is sorted
-// stably by key: the terms of one output block keep their generation order,
-// exactly as one global stable sort by key would leave them.
-static void finish_plan(Plan& P, std::vector<KeyTerm>& kt) {
-    const int nbr = P.nbr;
-    const int64_t nbc = P.nbc;
-    std::vector<int64_t> rp(nbr + 1, 0);
-    for (const KeyTerm& e : kt) rp[e.key / nbc + 1]++;
-    for (int i = 0; i < nbr; ++i) rp[i + 1] += rp[i];
-    std::vector<KeyTerm> s(kt.size());
-    {
-        std::vector<int64_t> pos(rp.begin(), rp.end() - 1);
-        for (const KeyTerm& e : kt) s[pos[e.key / nbc]++] = e;
-    }
-    std::vector<KeyTerm>().swap(kt);
-    std::vector<int> nk(nbr, 0);
-    parallel_for(nbr, 256, [&](int64_t i) {
-        auto b = s.begin() + rp[i], e = s.begin() + rp[i + 1];
-        std::stable_sort(b, e, [](const KeyTerm& x, const KeyTerm& y) { return x.key < y.key; });
-        int c = 0;
-        for (auto it = b; it != e; ++it)
-            if (it == b || it->key != (it - 1)->key) ++c;
-        nk[i] = c;
-    });
-    P.row_ptr.assign(nbr + 1, 0);
-    for (int i = 0; i < nbr; ++i) P.row_ptr[i + 1] = P.row_ptr[i] + nk[i];
-    const int nkeys = P.row_ptr[nbr];
-    P.col_idx.resize(nkeys);
-    P.tptr.assign((size_t)nkeys + 1, 0);
-    P.terms.resize(s.size());
-    parallel_for(nbr, 256, [&](int64_t i) {
-        int q = P.row_ptr[i] - 1;
-        for (int64_t t = rp[i]; t < rp[i + 1]; ++t) {
-            if (t == rp[i] || s[t].key != s[t - 1].key) {
-                ++q;
-                P.col_idx[q] = (int)(s[t].key - i * nbc);
-            }
-            P.tptr[q + 1]++;
-            P.terms[t] = s[t].t;
-        }
-    });
-    for (int o = 0; o < nkeys; ++o) P.tptr[o + 1] += P.tptr[o];
-}
-
-// Re-indexes P's terms onto the pattern of U (which holds P's pattern):
-// output blocks of U that P lacks get no terms.
-static void expand_plan(Plan& P, const Plan& U) {
-    std::vector<int> cnt((size_t)U.row_ptr[U.nbr], 0);
-    parallel_for(U.nbr, 256, [&](int64_t i) {
-        int p = P.row_ptr[i];
-        for (int q = U.row_ptr[i]; q < U.row_ptr[i + 1]; ++q)
-            if (p < P.row_ptr[i + 1] && P.col_idx[p] == U.col_idx[q]) {
-                cnt[q] = P.tptr[p + 1] - P.tptr[p];
-                ++p;
-            }
-        MG_REQUIRE(p == P.row_ptr[i + 1], MGLDG_ERR_SHAPE, "product pattern is not contained in the union");
-    });
-    P.row_ptr = U.row_ptr;
-    P.col_idx = U.col_idx;
-    P.tptr.assign(cnt.size() + 1, 0);
-    for (size_t q = 0; q < cnt.size(); ++q) P.tptr[q + 1] = P.tptr[q] + cnt[q];
-}
-
-// C = op(X) * Y   (multiply_mm when !tX, multiply_mm_t when tX)
-static Plan plan_mm(const mgldg_bsr* X, bool tX, const mgldg_bsr* Y) {
-    Clock clk(&g_plan_ms);
-    Plan P;
-    std::vector<KeyTerm> kt;
-    if (!tX) {
-        MG_REQUIRE(X->nbc == Y->nbr && X->bc == Y->br, MGLDG_ERR_SHAPE, "multiply_mm: shapes do not conform");
-        P.nbr = X->nbr; P.nbc = Y->nbc;
-        for (int i = 0; i < X->nbr; ++i)
-            for (int a = X->h_row_ptr[i]; a < X->h_row_ptr[i + 1]; ++a) {
-                int k = X->h_col_idx[a];
-                for (int b = Y->h_row_ptr[k]; b < Y->h_row_ptr[k + 1]; ++b)
-                    kt.push_back({(int64_t)i * P.nbc + Y->h_col_idx[b], Term{a, -1, b}});
-            }
-    } else {
-        MG_REQUIRE(X->nbr == Y->nbr && X->br == Y->br, MGLDG_ERR_SHAPE, "multiply_mm_t: shapes do not conform");
-        P.nbr = X->nbc; P.nbc = Y->nbc;
-        // column view of X: rows k of column i in ascending order
-        std::vector<int> cp(X->nbc + 1, 0);
-        for (int64_t a = 0; a < X->nnzb; ++a) cp[X->h_col_idx[a] + 1]++;
-        for (int j = 0; j < X->nbc; ++j) cp[j + 1] += cp[j];
-        std::vector<int> pos(cp.begin(), cp.end() - 1), ck(X->nnzb), ca(X->nnzb);
-        for (int k = 0; k < X->nbr; ++k)
-            for (int a = X->h_row_ptr[k]; a < X->h_row_ptr[k + 1]; ++a) {
-                int p = pos[X->h_col_idx[a]]++;
-                ck[p] = k;
-                ca[p] = a;
-            }
-        for (int i = 0; i < X->nbc; ++i)
-            for (int p = cp[i]; p < cp[i + 1]; ++p) {
-                int k = ck[p], a = ca[p];
-                for (int b = Y->h_row_ptr[k]; b < Y->h_row_ptr[k + 1]; ++b)
-                    kt.push_back({(int64_t)i * P.nbc + Y->h_col_idx[b], Term{a, -1, b}});
-            }
-    }
-    finish_plan(P, kt);
-    return P;
-}
-
-// sum over rows k of  X(k,i)^T D(k,k) X(k,j)  for i, j in cols(X, k):
-// the triple product of construct_laplacian (one dimension) and of the
-// coarse mass matrix.  `extra` adds output keys (the T pattern).
-static Plan plan_triple(const std::vector<const mgldg_bsr*>& Xs, const mgldg_bsr* D, const mgldg_bsr* extra,
-                        std::vector<Plan>* per_dim) {
-    Clock clk(&g_plan_ms);
-    const mgldg_bsr* X0 = Xs[0];
-    int nout = X0->nbc;
-    per_dim->clear();
-    for (size_t d = 0; d < Xs.size(); ++d) {
-        const mgldg_bsr* X = Xs[d];
-        MG_REQUIRE(X->nbr == D->nbr && X->br == D->bc, MGLDG_ERR_SHAPE, "triple product: shapes do not conform");
-        std::vector<KeyTerm> kt;
-        for (int k = 0; k < X->nbr; ++k) {
-            int m = D->h_diag[k];
-            MG_REQUIRE(m >= 0, MGLDG_ERR_SHAPE, "mass matrix lacks a diagonal block");
-            for (int a = X->h_row_ptr[k]; a < X->h_row_ptr[k + 1]; ++a)
-                for (int b = X->h_row_ptr[k]; b < X->h_row_ptr[k + 1]; ++b)
-                    kt.push_back({(int64_t)X->h_col_idx[a] * nout + X->h_col_idx[b], Term{a, m, b}});
-        }
-        Plan P;
-        P.nbr = nout; P.nbc = nout;
-        finish_plan(P, kt);
-        per_dim->push_back(std::move(P));
-    }
-    // the union pattern: every dimension's blocks and `extra`'s (the T pattern)
-    Plan U;
-    U.nbr = nout; U.nbc = nout;
-    std::vector<std::vector<int>> cols(nout);
-    parallel_for(nout, 256, [&](int64_t i) {
-        std::vector<int>& c = cols[i];
-        for (const Plan& P : *per_dim) c.insert(c.end(), P.col_idx.begin() + P.row_ptr[i], P.col_idx.begin() + P.row_ptr[i + 1]);
-        if (extra && i < extra->nbr)
-            c.insert(c.end(), extra->h_col_idx.begin() + extra->h_row_ptr[i], extra->h_col_idx.begin() + extra->h_row_ptr[i + 1]);
-        std::sort(c.begin(), c.end());
-        c.erase(std::unique(c.begin(), c.end()), c.end());
-    });
-    U.row_ptr.assign(nout + 1, 0);
-    for (int i = 0; i < nout; ++i) U.row_ptr[i + 1] = U.row_ptr[i] + (int)cols[i].size();
-    U.col_idx.resize(U.row_ptr[nout]);
-    parallel_for(nout, 256, [&](int64_t i) {
-        std::copy(cols[i].begin(), cols[i].end(), U.col_idx.begin() + U.row_ptr[i]);
-    });
-    U.tptr.assign((size_t)U.row_ptr[nout] + 1, 0);
-    for (Plan& P : *per_dim) expand_plan(P, U);
-    return U;
-}
 
 // ------------------------------------------------------------ numeric ------
 struct Opnd {
@@ -275,47 +108,33 @@ __global__ void __launch_bounds__(1024)
 
 static Opnd opnd(const mgldg_bsr* A) { return Opnd{A->val, A->blk, A->br, A->bc}; }
 
-static void run_plan(mgldg_ctx* ctx, const Plan& P, int oR, int oC, Opnd X, bool tX, Opnd Mm, Opnd Y,
+static void run_plan(mgldg_ctx* ctx, const DPlan& P, int oR, int oC, Opnd X, bool tX, Opnd Mm, Opnd Y,
                      const double* init, double* out) {
-    int nout = (int)P.col_idx.size();
+    const int nout = P.nkeys;
     if (nout == 0) return;
     Clock clk(&g_prod_ms);
     MG_REQUIRE(oR * oC <= 1024 && X.r * X.c <= 1024 && Y.r * Y.c <= 1024 && Mm.r * Mm.c <= 1024,
                MGLDG_ERR_UNSUPPORTED, "block products limited to 32x32 blocks");
-    int* dptr = nullptr;
-    int3* dterms = nullptr;
-    try {
-        dptr = dalloc<int>(P.tptr.size());
-        dterms = dalloc<int3>(std::max<size_t>(1, P.terms.size()));
-        upload(ctx, dptr, P.tptr.data(), P.tptr.size());
-        upload(ctx, dterms, reinterpret_cast<const int3*>(P.terms.data()), P.terms.size());
-        int nth = ((oR * oC + 31) / 32) * 32;
-        int grid = std::min(nout, 1 << 20);
-        {
-            Launch L(ctx, MGLDG_K_SETUP);
-            k_prod<<<grid, nth, 4 * 1024 * sizeof(double), ctx->stream>>>(nout, oR, oC, X, tX ? 1 : 0, Mm, Y, dptr,
-                                                                          dterms, init, out);
-        }
-        check_launch();
-        sync(ctx);
-    } catch (...) {
-        dfree(dptr);
-        dfree(dterms);
-        throw;
+    const int nth = ((oR * oC + 31) / 32) * 32;
+    const int grid = std::min(nout, 1 << 20);
+    {
+        Launch L(ctx, MGLDG_K_SETUP);
+        k_prod<<<grid, nth, 4 * 1024 * sizeof(double), ctx->stream>>>(nout, oR, oC, X, tX ? 1 : 0, Mm, Y, P.tptr,
+                                                                      P.terms, init, out);
     }
-    dfree(dptr);
-    dfree(dterms);
-}
-
-static mgldg_bsr* new_from_plan(mgldg_ctx* ctx, const Plan& P, int br, int bc) {
-    return bsr_new(ctx, P.nbr, P.nbc, br, bc, P.row_ptr, P.col_idx);
+    check_launch();
+    sync(ctx);
 }
 
 // C = op(X) * Y as a new BSR
 static mgldg_bsr* mm(mgldg_ctx* ctx, const mgldg_bsr* X, bool tX, const mgldg_bsr* Y) {
-    Plan P = plan_mm(X, tX, Y);
-    int oR = tX ? X->bc : X->br, oC = Y->bc;
-    mgldg_bsr* C = new_from_plan(ctx, P, oR, oC);
+    DPlan P;
+    {
+        Clock clk(&g_plan_ms);
+        dplan_mm(ctx, X, tX, Y, &P);
+    }
+    const int oR = tX ? X->bc : X->br, oC = Y->bc;
+    mgldg_bsr* C = bsr_from_dplan(ctx, P, oR, oC);
     try {
         run_plan(ctx, P, oR, oC, opnd(X), tX, Opnd{nullptr, nullptr, 0, 0}, opnd(Y), nullptr, C->val);
     } catch (...) {
@@ -491,24 +310,15 @@ __global__ void k_gather_blocks(int64_t n, int bsz, const int* __restrict__ src,
     }
 }
 
-static void gather_blocks(mgldg_ctx* ctx, const std::vector<int>& src_of, const mgldg_bsr* A, double* out) {
-    int64_t n = (int64_t)src_of.size();
+// out[q] = A's block src[q] for the n output positions (src on the device)
+static void gather_blocks(mgldg_ctx* ctx, int64_t n, const int* dsrc, const mgldg_bsr* A, double* out) {
     if (n == 0) return;
-    int* dsrc = dalloc<int>(n);
-    try {
-        upload(ctx, dsrc, src_of.data(), n);
-        int g = (int)std::min<int64_t>((n * (int64_t)A->bsz() + 255) / 256, ctx->sm_count * 32);
-        {
-            Launch L(ctx, MGLDG_K_SETUP);
-            k_gather_blocks<<<g, 256, 0, ctx->stream>>>(n, (int)A->bsz(), dsrc, A->val, A->blk, out);
-        }
-        check_launch();
-        sync(ctx);
-    } catch (...) {
-        dfree(dsrc);
-        throw;
+    const int g = (int)std::min<int64_t>((n * (int64_t)A->bsz() + 255) / 256, ctx->sm_count * 32);
+    {
+        Launch L(ctx, MGLDG_K_SETUP);
+        k_gather_blocks<<<g, 256, 0, ctx->stream>>>(n, (int)A->bsz(), dsrc, A->val, A->blk, out);
     }
-    dfree(dsrc);
+    check_launch();
 }
 
 // ------------------------------------------------------- construct_laplacian
@@ -516,23 +326,22 @@ static void gather_blocks(mgldg_ctx* ctx, const std::vector<int>& src_of, const 
 static mgldg_bsr* laplacian(mgldg_ctx* ctx, mgldg_bsr* M, mgldg_bsr* const* G, int ndim, mgldg_bsr* T) {
     bsr_build_diag(M);
     std::vector<const mgldg_bsr*> Xs(G, G + ndim);
-    std::vector<Plan> per;
-    Plan U = plan_triple(Xs, M, T, &per);
+    std::vector<DPlan> per;
+    DPlan U;
+    {
+        Clock clk(&g_plan_ms);
+        dplan_triple(ctx, Xs, M, T, &per, &U);
+    }
     const int b = T->br;
-    mgldg_bsr* A = new_from_plan(ctx, U, b, b);
+    mgldg_bsr* A = bsr_from_dplan(ctx, U, b, b);
     double* initv = nullptr;
+    int* dsrc = nullptr;
     try {
         // A starts as a copy of T scattered into the union pattern
-        initv = dalloc<double>(std::max<size_t>(1, U.col_idx.size() * A->bsz()));
-        std::vector<int> src_of(U.col_idx.size(), -1);
-        for (int i = 0; i < T->nbr; ++i) {
-            int q = U.row_ptr[i];
-            for (int a = T->h_row_ptr[i]; a < T->h_row_ptr[i + 1]; ++a) {
-                while (U.col_idx[q] != T->h_col_idx[a]) ++q;
-                src_of[q] = a;
-            }
-        }
-        gather_blocks(ctx, src_of, T, initv);
+        initv = dalloc<double>(std::max<size_t>(1, (size_t)U.nkeys * A->bsz()));
+        dsrc = dalloc<int>(std::max(1, U.nkeys));
+        dplan_scatter_index(ctx, U, T, dsrc);
+        gather_blocks(ctx, U.nkeys, dsrc, T, initv);
         double* src = initv;
         for (int d = 0; d < ndim; ++d) {
             run_plan(ctx, per[d], b, b, opnd(G[d]), true, opnd(M), opnd(G[d]), src, A->val);
@@ -540,9 +349,11 @@ static mgldg_bsr* laplacian(mgldg_ctx* ctx, mgldg_bsr* M, mgldg_bsr* const* G, i
         }
     } catch (...) {
         dfree(initv);
+        dfree(dsrc);
         delete A;
         throw;
     }
+    dfree(dsrc);
     dfree(initv);
     return A;
 }
@@ -575,9 +386,13 @@ mgldg_ops* galerkin_ratrat(mgldg_ctx* ctx, const mgldg_ops* f, const mgldg_bsr* 
     try {
         const int bc = T->bc;
         // coarse mass matrix (block diagonal): sum_k T(k,i)^T M(k,k) T(k,j)
-        std::vector<Plan> per;
-        Plan U = plan_triple({T}, f->M, nullptr, &per);
-        c->M = new_from_plan(ctx, U, bc, bc);
+        std::vector<DPlan> per;
+        DPlan U;
+        {
+            Clock clk(&g_plan_ms);
+            dplan_triple(ctx, {T}, f->M, nullptr, &per, &U);
+        }
+        c->M = bsr_from_dplan(ctx, U, bc, bc);
         run_plan(ctx, per[0], bc, bc, opnd(T), true, opnd(f->M), opnd(T), nullptr, c->M->val);
         bsr_build_diag(c->M);
         // Minv: inverses of the diagonal blocks of M_c
@@ -594,18 +409,9 @@ mgldg_ops* galerkin_ratrat(mgldg_ctx* ctx, const mgldg_ops* f, const mgldg_bsr* 
             mgldg_bsr* g = mm(ctx, T, true, t2);          // T^T M_f G_f T
             tmp.push_back(g);
             // G_c(i,j) = Minv_i G(i,j)
-            Plan P;
-            P.nbr = g->nbr; P.nbc = g->nbc;
-            P.row_ptr = g->h_row_ptr; P.col_idx = g->h_col_idx;
-            P.tptr.resize(g->nnzb + 1);
-            P.terms.resize(g->nnzb);
-            for (int i = 0; i < g->nbr; ++i)
-                for (int a = g->h_row_ptr[i]; a < g->h_row_ptr[i + 1]; ++a) {
-                    P.tptr[a] = a;
-                    P.terms[a] = Term{i, -1, a};
-                }
-            P.tptr[g->nnzb] = (int)g->nnzb;
-            c->G[d] = new_from_plan(ctx, P, bc, bc);
+            DPlan P;
+            dplan_rowscale(ctx, g, &P);
+            c->G[d] = bsr_new(ctx, g->nbr, g->nbc, bc, bc, g->h_row_ptr, g->h_col_idx);
             run_plan(ctx, P, bc, bc, Opnd{minv, nullptr, bc, bc}, false, Opnd{nullptr, nullptr, 0, 0}, opnd(g), nullptr,
                      c->G[d]->val);
             for (auto* m : tmp) delete m;
