@@ -195,10 +195,11 @@ def finish_cpu_baseline(proc):
 
 # ------------------------------------------------------------- GPU forms --
 def level_bytes(mg, nlev, s, f16=False):
-    """Per level: algorithmic bytes of one GS sweep, one Jacobi sweep, one SpMV.
-    f16: the level operator is read from its block-scaled FP16 copy (2 bytes
-    per entry + one 4-byte scale per block; inverse diagonal blocks and
-    vectors in FP32, s = 4)."""
+    """Per level: algorithmic bytes of one GS sweep, one Jacobi sweep, one
+    Jacobi sweep from x = 0 (the first of each V-cycle level: inverse diagonal
+    blocks, b and x_out only), one SpMV.  f16: the level operator is read from
+    its block-scaled FP16 copy (2 bytes per entry + one 4-byte scale per
+    block; inverse diagonal blocks and vectors in FP32, s = 4)."""
     out = []
     for l in range(nlev):
         nbr, nbc, br, bc, nnzb = mg.level_op(l, 4).info()
@@ -208,8 +209,9 @@ def level_bytes(mg, nlev, s, f16=False):
         av = nnzb * (b2 * 2 + 4) if f16 else nnzb * b2 * s
         gs = (nnzb - nbr) * b2 * s + nbr * b2 * s + idx + 3 * n * s
         jac = av + nbr * b2 * s + idx + 3 * n * s
+        jac0 = nbr * b2 * s + 2 * n * s
         spmv = av + idx + 3 * n * s
-        out.append(dict(gs=gs, jacobi=jac, spmv=spmv, nbr=nbr, nnzb=nnzb, b=br))
+        out.append(dict(gs=gs, jacobi=jac, jacobi0=jac0, spmv=spmv, nbr=nbr, nnzb=nnzb, b=br))
     return out
 
 
@@ -841,8 +843,12 @@ def run_gpu(args, ws, rank, local):
         lb = level_bytes(mgs[form], levels - 1, 4 if prec in (1, 2) else 8, f16=prec == 2)
         n0, ms0 = per_level_f[cls][0]
         # a Gauss-Seidel launch is a pass of npre (= npost) sweeps, each
-        # reading the level's blocks once
+        # reading the level's blocks once; of the npre + npost Jacobi launches
+        # per V-cycle the first starts from x = 0 and reads no operator
         bytes0 = lb[0][key] * (WL["npre"] if key == "gs" else 1)
+        if key == "jacobi":
+            nsw = WL["npre"] + WL["npost"]
+            bytes0 = ((nsw - 1) * lb[0]["jacobi"] + lb[0]["jacobi0"]) / nsw
         achieved = bytes0 * n0 / (ms0 * 1e-3) / 1e9
         r = {"bound": "hbm", "form": form, "kernel": cls, "level": 0, "achieved": achieved, "peak": hbm,
              "unit": "GB/s", "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind, "launches": n0,

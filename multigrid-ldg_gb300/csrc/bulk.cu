@@ -154,13 +154,17 @@ __device__ __forceinline__ float row_from(const __half* a, const float* scl, con
     return acc;
 }
 
-// JACOBI: xout_i = xin_i + omega * Dinv_i (b_i - (A xin)_i)
+// JACOBI: xout_i = xin_i + omega * Dinv_i (b_i - (A xin)_i); with xzero
+//         (xin = 0) only the inverse diagonal blocks are staged and neither
+//         A nor xin is read: (A 0)_i is +0, so the values are the full
+//         sweep's bit for bit
 // else:   y_i = alpha (A x)_i + beta yin_i
 template <bool JACOBI, class VT>
 __global__ void __launch_bounds__(kRows * 32, Stage<VT>::kMinBlocks)
     k_rows_bulk(int nbr, const int* __restrict__ row_ptr, const int* __restrict__ col_idx, const VT* __restrict__ val,
                 const float* __restrict__ scale, const float* __restrict__ Dinv, const float* __restrict__ x,
-                const float* bvec, float* y, float alpha, float beta, float omega, unsigned* err, int64_t timeout_ns) {
+                const float* bvec, float* y, float alpha, float beta, float omega, bool xzero, unsigned* err,
+                int64_t timeout_ns) {
     using S = Stage<VT>;
     constexpr bool kF16 = sizeof(VT) == 2;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -204,7 +208,7 @@ __global__ void __launch_bounds__(kRows * 32, Stage<VT>::kMinBlocks)
         const int cstart = k0 & ~3;
         const int ncol = ((k1 - cstart) + 3) & ~3;
         s_col0[st] = cstart;
-        const bool copy_rows = fits && nbk > 0;
+        const bool copy_rows = fits && nbk > 0 && !xzero;
         unsigned bytes = 0;
         if (copy_rows) bytes += (unsigned)nbk * kBlk * sizeof(VT) + (unsigned)ncol * sizeof(int) * (kF16 ? 2 : 1);
         if (JACOBI) bytes += (unsigned)(r1 - r0) * kBlk * sizeof(float);
@@ -247,7 +251,7 @@ __global__ void __launch_bounds__(kRows * 32, Stage<VT>::kMinBlocks)
             float bi = 0.f, xi = 0.f;
             if (JACOBI && (lane & 1) == 0) {
                 bi = __ldg(bvec + (size_t)row * kB + r);
-                xi = __ldg(x + (size_t)row * kB + r);
+                if (!xzero) xi = __ldg(x + (size_t)row * kB + r);
             }
             const bool fits = s_fits[st] != 0;
             const VT* a = fits ? reinterpret_cast<const VT*>(sv) + (size_t)(k0 - kg) * kBlk : val + (size_t)k0 * kBlk;
@@ -255,8 +259,11 @@ __global__ void __launch_bounds__(kRows * 32, Stage<VT>::kMinBlocks)
             const float* scl = kF16 ? (fits ? reinterpret_cast<const float*>(sv + S::kScl) + (k0 - s_col0[st])
                                             : scale + k0)
                                     : nullptr;
-            float acc = row_from(a, scl, cols, x, k1 - k0, r, c0, lane);
-            acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+            float acc = 0.f;
+            if (!(JACOBI && xzero)) {
+                acc = row_from(a, scl, cols, x, k1 - k0, r, c0, lane);
+                acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+            }
             if (JACOBI) {
                 const float t = bi - acc;   // valid in even lanes
                 const float4* dp =
@@ -309,9 +316,52 @@ __global__ void __launch_bounds__(kRows * 32, Stage<VT>::kMinBlocks)
     }
 }
 
+// The first Jacobi sweep from x = 0 on 16 x 16 blocks: x_i = omega Dinv_i b_i
+// with the bulk kernel's lane layout and arithmetic (lane pair 2r, 2r+1 holds
+// row r, eight columns each; the same fma chain and pair sum), so the values
+// are its xzero values bit for bit.  Only Dinv and b are read -- a plain
+// coalesced stream (1 KiB of Dinv per row and warp), which needs no staging.
+__global__ void __launch_bounds__(256) k_jacobi_zero16(int nbr, const float* __restrict__ Dinv,
+                                                       const float* __restrict__ bvec, float* __restrict__ y,
+                                                       float omega) {
+    const int lane = threadIdx.x & 31;
+    const int r = lane >> 1, c0 = (lane & 1) * 8;
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    for (int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < nbr; row += nw) {
+        const float4* dp = reinterpret_cast<const float4*>(Dinv + (size_t)row * kBlk + r * kB + c0);
+        const float4 d0 = __ldg(dp), d1 = __ldg(dp + 1);
+        const float t = ((lane & 1) == 0) ? __ldg(bvec + (size_t)row * kB + r) : 0.f;   // b - (A 0) = b
+        float tc[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) tc[c] = __shfl_sync(0xffffffffu, t, ((c0 + c) * 2) & 31);
+        float yv = d0.x * tc[0];
+        yv = fmaf(d0.y, tc[1], yv);
+        yv = fmaf(d0.z, tc[2], yv);
+        yv = fmaf(d0.w, tc[3], yv);
+        yv = fmaf(d1.x, tc[4], yv);
+        yv = fmaf(d1.y, tc[5], yv);
+        yv = fmaf(d1.z, tc[6], yv);
+        yv = fmaf(d1.w, tc[7], yv);
+        yv += __shfl_xor_sync(0xffffffffu, yv, 1);
+        const float xi = 0.f;
+        if ((lane & 1) == 0) y[(size_t)row * kB + r] = xi + omega * yv;
+    }
+}
+
+static void launch_jacobi_zero16(mgldg_ctx* ctx, const mgldg_bsr* A, const float* Dinv, const float* b, float* xout,
+                                 float omega) {
+    const int grid = std::max(1, std::min((A->nbr + 7) / 8, ctx->sm_count * 8));
+    {
+        Launch L(ctx, MGLDG_K_JACOBI);
+        k_jacobi_zero16<<<grid, 256, 0, ctx->stream>>>(A->nbr, Dinv, b, xout, omega);
+    }
+    check_launch();
+}
+
 template <bool JACOBI, class VT>
 static void launch_bulk(mgldg_ctx* ctx, const mgldg_bsr* A, const VT* vals, const float* scale, const float* Dinv,
-                        const float* x, const float* bvec, float* y, float alpha, float beta, float omega, int kclass) {
+                        const float* x, const float* bvec, float* y, float alpha, float beta, float omega, bool xzero,
+                        int kclass) {
     static bool attr_set[64] = {false};
     if (ctx->device < 64 && !attr_set[ctx->device]) {
         MG_CHECK_CUDA(cudaFuncSetAttribute(k_rows_bulk<JACOBI, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -323,7 +373,8 @@ static void launch_bulk(mgldg_ctx* ctx, const mgldg_bsr* A, const VT* vals, cons
     {
         Launch L(ctx, kclass);
         k_rows_bulk<JACOBI, VT><<<grid, kRows * 32, Stage<VT>::kSmem, ctx->stream>>>(
-            A->nbr, A->row_ptr, A->col_idx, vals, scale, Dinv, x, bvec, y, alpha, beta, omega, ctx->d_err, 1000000000LL);
+            A->nbr, A->row_ptr, A->col_idx, vals, scale, Dinv, x, bvec, y, alpha, beta, omega, xzero, ctx->d_err,
+            1000000000LL);
     }
     check_launch();
 }
@@ -331,28 +382,31 @@ static void launch_bulk(mgldg_ctx* ctx, const mgldg_bsr* A, const VT* vals, cons
 bool bulk_spmv_f32(mgldg_ctx* ctx, const mgldg_bsr* A, float alpha, const float* x, float beta, const float* yin,
                    float* y, int kclass) {
     if (A->br != kB || A->bc != kB || A->blk || !A->val32 || A->nbr == 0) return false;
-    launch_bulk<false, float>(ctx, A, A->val32, nullptr, nullptr, x, yin, y, alpha, beta, 0.f, kclass);
+    launch_bulk<false, float>(ctx, A, A->val32, nullptr, nullptr, x, yin, y, alpha, beta, 0.f, false, kclass);
     return true;
 }
 
 bool bulk_spmv_f16(mgldg_ctx* ctx, const mgldg_bsr* A, float alpha, const float* x, float beta, const float* yin,
                    float* y, int kclass) {
     if (A->br != kB || A->bc != kB || A->blk || !A->val16 || A->nbr == 0) return false;
-    launch_bulk<false, __half>(ctx, A, A->val16, A->scale16, nullptr, x, yin, y, alpha, beta, 0.f, kclass);
+    launch_bulk<false, __half>(ctx, A, A->val16, A->scale16, nullptr, x, yin, y, alpha, beta, 0.f, false, kclass);
     return true;
 }
 
 bool bulk_jacobi_f16(mgldg_ctx* ctx, const mgldg_bsr* A, const float* Dinv, const float* b, const float* xin,
-                     float* xout, float omega) {
+                     float* xout, float omega, bool xzero) {
     if (A->br != kB || A->bc != kB || A->blk || !A->val16 || A->nbr == 0) return false;
-    launch_bulk<true, __half>(ctx, A, A->val16, A->scale16, Dinv, xin, b, xout, 0.f, 0.f, omega, MGLDG_K_JACOBI);
+    if (xzero) launch_jacobi_zero16(ctx, A, Dinv, b, xout, omega);
+    else launch_bulk<true, __half>(ctx, A, A->val16, A->scale16, Dinv, xin, b, xout, 0.f, 0.f, omega, false,
+                                   MGLDG_K_JACOBI);
     return true;
 }
 
 bool bulk_jacobi_f32(mgldg_ctx* ctx, const mgldg_bsr* A, const float* vals, const float* Dinv, const float* b,
-                     const float* xin, float* xout, float omega) {
+                     const float* xin, float* xout, float omega, bool xzero) {
     if (A->br != kB || A->bc != kB || A->blk || A->nbr == 0) return false;
-    launch_bulk<true, float>(ctx, A, vals, nullptr, Dinv, xin, b, xout, 0.f, 0.f, omega, MGLDG_K_JACOBI);
+    if (xzero) launch_jacobi_zero16(ctx, A, Dinv, b, xout, omega);
+    else launch_bulk<true, float>(ctx, A, vals, nullptr, Dinv, xin, b, xout, 0.f, 0.f, omega, false, MGLDG_K_JACOBI);
     return true;
 }
 

@@ -212,7 +212,7 @@ void bsr_ensure_lo32(mgldg_bsr* A);
 bool spmv_f16(mgldg_ctx* ctx, const mgldg_bsr* A, float alpha, const float* x, float beta, const float* yin, float* y,
               int kclass);
 bool jacobi_f16(mgldg_ctx* ctx, const mgldg_bsr* A, const float* Dinv, const float* b, const float* xin, float* xout,
-                float omega);
+                float omega, bool xzero = false);
 // block sizes read from the FP16 copy: 16x16 only.  The small-block kernels
 // (3..10) are bound by load latency rather than bytes, and an FP16 copy made
 // them slower (392k-triangle disk solve 53 -> 72 ms), so those levels keep
@@ -256,11 +256,11 @@ void dense_spd_inverse(mgldg_ctx* ctx, const mgldg_bsr* A, double* out_inv);
 bool bulk_spmv_f32(mgldg_ctx* ctx, const mgldg_bsr* A, float alpha, const float* x, float beta, const float* yin,
                    float* y, int kclass);
 bool bulk_jacobi_f32(mgldg_ctx* ctx, const mgldg_bsr* A, const float* vals, const float* Dinv, const float* b,
-                     const float* xin, float* xout, float omega);
+                     const float* xin, float* xout, float omega, bool xzero = false);
 bool bulk_spmv_f16(mgldg_ctx* ctx, const mgldg_bsr* A, float alpha, const float* x, float beta, const float* yin,
                    float* y, int kclass);
 bool bulk_jacobi_f16(mgldg_ctx* ctx, const mgldg_bsr* A, const float* Dinv, const float* b, const float* xin,
-                     float* xout, float omega);
+                     float* xout, float omega, bool xzero = false);
 // reads and clears the device error word; throws MGLDG_ERR_TIMEOUT if set
 void take_device_error(mgldg_ctx* ctx);
 

@@ -92,11 +92,11 @@ __global__ void k_mean_project(int n, T* b) {
 // ----------------------------------------------------------------- V-cycle --
 // the FP16-copy forms of the level products (FP32 vectors only)
 template <class T>
-static bool jacobi_f16_t(mgldg_ctx*, const mgldg_bsr*, const T*, const T*, const T*, T*, T) { return false; }
+static bool jacobi_f16_t(mgldg_ctx*, const mgldg_bsr*, const T*, const T*, const T*, T*, T, bool) { return false; }
 template <>
 bool jacobi_f16_t<float>(mgldg_ctx* ctx, const mgldg_bsr* A, const float* D, const float* b, const float* xin,
-                         float* xout, float omega) {
-    return jacobi_f16(ctx, A, D, b, xin, xout, omega);
+                         float* xout, float omega, bool xzero) {
+    return jacobi_f16(ctx, A, D, b, xin, xout, omega, xzero);
 }
 template <class T>
 static bool spmv_f16_t(mgldg_ctx*, const mgldg_bsr*, T, const T*, T, const T*, T*) { return false; }
@@ -106,8 +106,10 @@ bool spmv_f16_t<float>(mgldg_ctx* ctx, const mgldg_bsr* A, float alpha, const fl
     return spmv_f16(ctx, A, alpha, x, beta, yin, y, MGLDG_K_SPMV);
 }
 
+// n smoothing sweeps on level i; xzero: the level's x is the zero vector
+// (not materialised: only the Jacobi smoother takes it, see zero_start)
 template <class T>
-static void relax(mgldg_mg* m, int i, int n, bool reverse) {
+static void relax(mgldg_mg* m, int i, int n, bool reverse, bool xzero = false) {
     LevelData& L = m->L[i];
     m->ctx->cur_level = i;
     const T* vals = bsr_vals<T>(L.A);
@@ -118,15 +120,27 @@ static void relax(mgldg_mg* m, int i, int n, bool reverse) {
         return;
     }
     for (int k = 0; k < n; ++k) {
+        const bool z = xzero && k == 0;
         if (!(f16 && jacobi_f16_t<T>(m->ctx, L.A, LV<T>::D(L), LV<T>::b(L), LV<T>::x(L), LV<T>::xt(L),
-                                      (T)m->p.omega)))
-            jacobi_sweep<T>(m->ctx, L.A, vals, LV<T>::D(L), LV<T>::b(L), LV<T>::x(L), LV<T>::xt(L), (T)m->p.omega);
+                                      (T)m->p.omega, z)))
+            jacobi_sweep<T>(m->ctx, L.A, vals, LV<T>::D(L), LV<T>::b(L), LV<T>::x(L), LV<T>::xt(L), (T)m->p.omega,
+                            z);
         std::swap(LV<T>::x(L), LV<T>::xt(L));
     }
 }
 
+// True when level i starts a V-cycle from x = 0 with a Jacobi sweep, which
+// then reads neither x nor A (the V-cycle skips zeroing x as well): every
+// level but a directly solved coarsest one, with npre >= 1.  Gauss-Seidel
+// reads the old values of the rows after the current one, so its x stays
+// materialised.
+static bool zero_start(const mgldg_mg* m, int i) {
+    if (m->p.relaxation != MGLDG_RELAX_JACOBI || m->p.npre < 1) return false;
+    return i < (int)m->L.size() - 1 || m->p.solver == MGLDG_COARSE_RELAXATION;
+}
+
 template <class T>
-static void coarse_solve(mgldg_mg* m, int i) {
+static void coarse_solve(mgldg_mg* m, int i, bool xzero) {
     LevelData& L = m->L[i];
     mgldg_ctx* ctx = m->ctx;
     ctx->cur_level = i;
@@ -136,7 +150,7 @@ static void coarse_solve(mgldg_mg* m, int i) {
             k_mean_project<T><<<1, 1024, 0, ctx->stream>>>((int)L.n, LV<T>::b(L));
         }
         check_launch();
-        relax<T>(m, i, m->p.npre, false);
+        relax<T>(m, i, m->p.npre, false, xzero);
         relax<T>(m, i, m->p.npost, true);
         return;
     }
@@ -153,16 +167,17 @@ static void coarse_solve(mgldg_mg* m, int i) {
     check_launch();
 }
 
+// xzero: level i's x is zero and not materialised (zero_start(m, i))
 template <class T>
-static void vcycle(mgldg_mg* m, int i) {
+static void vcycle(mgldg_mg* m, int i, bool xzero) {
     mgldg_ctx* ctx = m->ctx;
     if (i == (int)m->L.size() - 1) {
-        coarse_solve<T>(m, i);
+        coarse_solve<T>(m, i, xzero);
         return;
     }
     LevelData& L = m->L[i];
     LevelData& C = m->L[i + 1];
-    relax<T>(m, i, m->p.npre, false);
+    relax<T>(m, i, m->p.npre, false, xzero);
     // r = b - A x ; b_c = T^T r ; x_c = 0
     ctx->cur_level = i;
     if (!(m->p.precision == MGLDG_PREC_MIXED_F16 &&
@@ -170,8 +185,9 @@ static void vcycle(mgldg_mg* m, int i) {
         spmv<T>(ctx, L.A, T(-1), LV<T>::x(L), T(1), LV<T>::b(L), LV<T>::r(L));
     spmv<T>(ctx, L.Tt, T(1), LV<T>::r(L), T(0), (const T*)nullptr, LV<T>::b(C), nullptr, nullptr, nullptr,
             MGLDG_K_TRANSFER);
-    MG_CHECK_CUDA(cudaMemsetAsync(LV<T>::x(C), 0, C.n * sizeof(T), ctx->stream));
-    vcycle<T>(m, i + 1);
+    const bool czero = zero_start(m, i + 1);
+    if (!czero) MG_CHECK_CUDA(cudaMemsetAsync(LV<T>::x(C), 0, C.n * sizeof(T), ctx->stream));
+    vcycle<T>(m, i + 1, czero);
     // x += T x_c
     ctx->cur_level = i;
     spmv<T>(ctx, L.T, T(1), LV<T>::x(C), T(1), LV<T>::x(L), LV<T>::x(L), nullptr, nullptr, nullptr, MGLDG_K_TRANSFER);
@@ -231,16 +247,19 @@ static void vcycle_dev(mgldg_mg* m, const double* b, double* x, bool x_is_zero, 
     } reset{ctx};
     if (m->p.precision != MGLDG_PREC_FP64) {
         convert<double, float>(ctx, L.n, b, L.b32);
-        if (x_is_zero) MG_CHECK_CUDA(cudaMemsetAsync(L.x32, 0, L.n * sizeof(float), ctx->stream));
-        else convert<double, float>(ctx, L.n, x, L.x32);
-        vcycle<float>(m, 0);
+        const bool z = x_is_zero && zero_start(m, 0);
+        if (x_is_zero && !z) MG_CHECK_CUDA(cudaMemsetAsync(L.x32, 0, L.n * sizeof(float), ctx->stream));
+        else if (!x_is_zero) convert<double, float>(ctx, L.n, x, L.x32);
+        vcycle<float>(m, 0, z);
         if (dot_part) out_dot<float>(ctx, L.n, L.x32, b, x, dot_part);
         else convert<float, double>(ctx, L.n, L.x32, x);
     } else {
         MG_CHECK_CUDA(cudaMemcpyAsync(L.bb, b, L.n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-        if (x_is_zero) MG_CHECK_CUDA(cudaMemsetAsync(L.x, 0, L.n * sizeof(double), ctx->stream));
-        else MG_CHECK_CUDA(cudaMemcpyAsync(L.x, x, L.n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-        vcycle<double>(m, 0);
+        const bool z = x_is_zero && zero_start(m, 0);
+        if (x_is_zero && !z) MG_CHECK_CUDA(cudaMemsetAsync(L.x, 0, L.n * sizeof(double), ctx->stream));
+        else if (!x_is_zero)
+            MG_CHECK_CUDA(cudaMemcpyAsync(L.x, x, L.n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+        vcycle<double>(m, 0, z);
         if (dot_part) out_dot<double>(ctx, L.n, L.x, b, x, dot_part);
         else MG_CHECK_CUDA(cudaMemcpyAsync(x, L.x, L.n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
     }

@@ -414,11 +414,16 @@ __global__ void __launch_bounds__(WPB * 32)
 
 // ------------------------------------------------------------ Jacobi sweep --
 // x_out_i = x_in_i + omega * Dinv_i (b_i - sum_j A_ij x_in_j)
+//
+// xzero: x_in is the zero vector (the first sweep of a V-cycle level), so
+// the kernels neither read A nor x_in.  The product of A with zeros is +0 in
+// every lane and b_i - (+0) = b_i, so the sweep still gives the full
+// sweep's values bit for bit.
 template <class T, int B, int WPB>
 __global__ void __launch_bounds__(WPB * 32, 2)
     k_jacobi(int n, const int* __restrict__ row_ptr, const int* __restrict__ col_idx, const T* __restrict__ val,
              const T* __restrict__ Dinv, const T* __restrict__ b, const T* __restrict__ xin, T* __restrict__ xout,
-             T omega) {
+             T omega, bool xzero) {
     using L = WL<B, B>;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int r = lane / L::S, s = lane - r * L::S;
@@ -429,15 +434,18 @@ __global__ void __launch_bounds__(WPB * 32, 2)
         T bi = 0, xi = 0;
         if (active && s == 0) {
             bi = __ldg(b + (size_t)i * B + r);
-            xi = __ldg(xin + (size_t)i * B + r);
+            if (!xzero) xi = __ldg(xin + (size_t)i * B + r);
         }
         T dch[L::CH];
         const T* Di = Dinv + (size_t)i * B * B;
 #pragma unroll
         for (int c = 0; c < L::CH; ++c) dch[c] = (active && c0 + c < B) ? __ldg(Di + r * B + c0 + c) : T(0);
-        const int k0 = __ldg(row_ptr + i), k1 = __ldg(row_ptr + i + 1);
-        T acc = row_product<T, B, B>(col_idx, val, nullptr, xin, k0, k1, r, c0, active, lane);
-        acc = seg_sum<L::S>(acc);
+        T acc = 0;
+        if (!xzero) {
+            const int k0 = __ldg(row_ptr + i), k1 = __ldg(row_ptr + i + 1);
+            acc = row_product<T, B, B>(col_idx, val, nullptr, xin, k0, k1, r, c0, active, lane);
+            acc = seg_sum<L::S>(acc);
+        }
         const T t = (active && s == 0) ? bi - acc : T(0);
         T y = 0;
 #pragma unroll
@@ -460,7 +468,7 @@ template <class T, class VT, int B, int MAXB>
 __global__ void __launch_bounds__(256)
     k_jacobi_rows(int n, const int* __restrict__ row_ptr, const int* __restrict__ col_idx, const VT* __restrict__ val,
                   const float* __restrict__ scl, const T* __restrict__ Dinv, const T* __restrict__ b,
-                  const T* __restrict__ xin, T* __restrict__ xout, T omega) {
+                  const T* __restrict__ xin, T* __restrict__ xout, T omega, bool xzero) {
     using R = Rows<B>;
     __shared__ T sr[8 * R::SM];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -477,9 +485,11 @@ __global__ void __launch_bounds__(256)
         T bi = 0, xi = 0;
         if (valid) {
             bi = __ldg(b + o);
-            xi = __ldg(xin + o);
-            cols_accumulate<T, VT, B, B, MAXB>(col_idx, val, scl, nullptr, xin, __ldg(row_ptr + row),
-                                               __ldg(row_ptr + row + 1), c, acc);
+            if (!xzero) {
+                xi = __ldg(xin + o);
+                cols_accumulate<T, VT, B, B, MAXB>(col_idx, val, scl, nullptr, xin, __ldg(row_ptr + row),
+                                                   __ldg(row_ptr + row + 1), c, acc);
+            }
         }
         const T t = bi - rows_reduce<T, B, B>(acc, s, g, c, g < R::G);
         // lane (g, c) now holds t_c; y_c = sum_k Dinv(c, k) t_k
@@ -497,14 +507,14 @@ __global__ void __launch_bounds__(256)
 
 template <class T, int B, class VT = T>
 static void launch_jacobi_rows(mgldg_ctx* ctx, const mgldg_bsr* A, const VT* vals, const T* Dinv, const T* b,
-                               const T* xin, T* xout, T omega, const float* scl = nullptr) {
+                               const T* xin, T* xout, T omega, bool xzero, const float* scl = nullptr) {
     constexpr int MAXB = (sizeof(T) == 4 || B <= 4) ? 4 : 2;
     const int rows_per_cta = 8 * Rows<B>::G;
     const int grid = std::max(1, std::min((A->nbr + rows_per_cta - 1) / rows_per_cta, ctx->sm_count * 8));
     {
         Launch L(ctx, MGLDG_K_JACOBI);
         k_jacobi_rows<T, VT, B, MAXB><<<grid, 256, 0, ctx->stream>>>(A->nbr, A->row_ptr, A->col_idx, vals, scl, Dinv,
-                                                                     b, xin, xout, omega);
+                                                                     b, xin, xout, omega, xzero);
     }
     check_launch();
 }
@@ -757,56 +767,56 @@ template void gs_sweeps<float>(mgldg_ctx*, const mgldg_bsr*, const float*, const
 
 template <class T, int B>
 static void launch_jacobi(mgldg_ctx* ctx, const mgldg_bsr* A, const T* vals, const T* Dinv, const T* b,
-                          const T* xin, T* xout, T omega) {
+                          const T* xin, T* xout, T omega, bool xzero) {
     constexpr int WPB = 8;
     int grid = std::max(1, std::min((A->nbr + WPB - 1) / WPB, ctx->sm_count * 16));
     {
         Launch L(ctx, MGLDG_K_JACOBI);
         k_jacobi<T, B, WPB><<<grid, WPB * 32, 0, ctx->stream>>>(A->nbr, A->row_ptr, A->col_idx, vals, Dinv, b, xin,
-                                                                xout, omega);
+                                                                xout, omega, xzero);
     }
     check_launch();
 }
 
 template <class T>
 void jacobi_sweep(mgldg_ctx* ctx, const mgldg_bsr* A, const T* vals, const T* Dinv, const T* b, const T* xin,
-                  T* xout, T omega) {
+                  T* xout, T omega, bool xzero) {
     if (A->nbr == 0) return;
     if constexpr (std::is_same<T, float>::value) {
-        if (bulk_jacobi_f32(ctx, A, vals, Dinv, b, xin, xout, omega)) return;
+        if (bulk_jacobi_f32(ctx, A, vals, Dinv, b, xin, xout, omega, xzero)) return;
     }
     if (!A->blk) switch (A->br) {
-            case 3: launch_jacobi_rows<T, 3>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
-            case 4: launch_jacobi_rows<T, 4>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
-            case 6: launch_jacobi_rows<T, 6>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
-            case 8: launch_jacobi_rows<T, 8>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
-            case 9: launch_jacobi_rows<T, 9>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
-            case 10: launch_jacobi_rows<T, 10>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
+            case 3: launch_jacobi_rows<T, 3>(ctx, A, vals, Dinv, b, xin, xout, omega, xzero); return;
+            case 4: launch_jacobi_rows<T, 4>(ctx, A, vals, Dinv, b, xin, xout, omega, xzero); return;
+            case 6: launch_jacobi_rows<T, 6>(ctx, A, vals, Dinv, b, xin, xout, omega, xzero); return;
+            case 8: launch_jacobi_rows<T, 8>(ctx, A, vals, Dinv, b, xin, xout, omega, xzero); return;
+            case 9: launch_jacobi_rows<T, 9>(ctx, A, vals, Dinv, b, xin, xout, omega, xzero); return;
+            case 10: launch_jacobi_rows<T, 10>(ctx, A, vals, Dinv, b, xin, xout, omega, xzero); return;
         }
     switch (A->br) {
-        case 1: launch_jacobi<T, 1>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
-        case 3: launch_jacobi<T, 3>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
-        case 4: launch_jacobi<T, 4>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
-        case 6: launch_jacobi<T, 6>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
-        case 8: launch_jacobi<T, 8>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
-        case 9: launch_jacobi<T, 9>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
-        case 10: launch_jacobi<T, 10>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
-        case 16: launch_jacobi<T, 16>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
-        case 25: launch_jacobi<T, 25>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
-        case 27: launch_jacobi<T, 27>(ctx, A, vals, Dinv, b, xin, xout, omega); return;
+        case 1: launch_jacobi<T, 1>(ctx, A, vals, Dinv, b, xin, xout, omega, xzero); return;
+        case 3: launch_jacobi<T, 3>(ctx, A, vals, Dinv, b, xin, xout, omega, xzero); return;
+        case 4: launch_jacobi<T, 4>(ctx, A, vals, Dinv, b, xin, xout, omega, xzero); return;
+        case 6: launch_jacobi<T, 6>(ctx, A, vals, Dinv, b, xin, xout, omega, xzero); return;
+        case 8: launch_jacobi<T, 8>(ctx, A, vals, Dinv, b, xin, xout, omega, xzero); return;
+        case 9: launch_jacobi<T, 9>(ctx, A, vals, Dinv, b, xin, xout, omega, xzero); return;
+        case 10: launch_jacobi<T, 10>(ctx, A, vals, Dinv, b, xin, xout, omega, xzero); return;
+        case 16: launch_jacobi<T, 16>(ctx, A, vals, Dinv, b, xin, xout, omega, xzero); return;
+        case 25: launch_jacobi<T, 25>(ctx, A, vals, Dinv, b, xin, xout, omega, xzero); return;
+        case 27: launch_jacobi<T, 27>(ctx, A, vals, Dinv, b, xin, xout, omega, xzero); return;
     }
     throw Error(MGLDG_ERR_UNSUPPORTED, "Jacobi: unsupported block size");
 }
 bool jacobi_f16(mgldg_ctx* ctx, const mgldg_bsr* A, const float* Dinv, const float* b, const float* xin, float* xout,
-                float omega) {
+                float omega, bool xzero) {
     if (!A->val16 || A->blk || A->nbr == 0 || !f16_shape(A->br, A->bc)) return false;
-    return bulk_jacobi_f16(ctx, A, Dinv, b, xin, xout, omega);
+    return bulk_jacobi_f16(ctx, A, Dinv, b, xin, xout, omega, xzero);
 }
 
 template void jacobi_sweep<double>(mgldg_ctx*, const mgldg_bsr*, const double*, const double*, const double*,
-                                   const double*, double*, double);
+                                   const double*, double*, double, bool);
 template void jacobi_sweep<float>(mgldg_ctx*, const mgldg_bsr*, const float*, const float*, const float*, const float*,
-                                  float*, float);
+                                  float*, float, bool);
 
 }  // namespace mg
 

@@ -44,8 +44,10 @@ int gs_take_error(mgldg_ctx* ctx, Sched& S);
 template <class T>
 void gs_sweeps(mgldg_ctx* ctx, const mgldg_bsr* A, const T* vals, const T* Dinv, const T* b, T* x, Sched& S, T omega,
                bool reverse, int nsw);
+// one damped block-Jacobi sweep xin -> xout; xzero: xin is the zero vector
+// (neither it nor A is read; same values as the full sweep)
 template <class T>
 void jacobi_sweep(mgldg_ctx* ctx, const mgldg_bsr* A, const T* vals, const T* Dinv, const T* b, const T* xin,
-                  T* xout, T omega);
+                  T* xout, T omega, bool xzero = false);
 
 }  // namespace mg
