@@ -46,6 +46,9 @@ struct SpmmArgs {
     const T* Dinv;
     const T* B;
     T omega;
+    // Jacobi from X = 0: neither X nor A is read ((A 0)_i is +0, so the
+    // values are the full sweep's bit for bit)
+    int xzero;
 };
 
 template <class T, int V>
@@ -166,7 +169,7 @@ __global__ void __launch_bounds__(256) k_spmm(const SpmmArgs<T> a) {
         for (int r = 0; r < BR; ++r)
 #pragma unroll
             for (int v = 0; v < V; ++v) acc[r][v] = T(0);
-        const int k0 = a.row_ptr[i], k1 = a.row_ptr[i + 1];
+        const int k0 = a.row_ptr[i], k1 = (MODE == 1 && a.xzero) ? k0 : a.row_ptr[i + 1];
         T pre[S::PER];
         if (k0 < k1) stage_fetch<T, BR, BC>(a.val + (size_t)(a.blk ? a.blk[k0] : k0) * (BR * BC), lane, pre);
         for (int kk = k0; kk < k1; ++kk) {
@@ -228,7 +231,12 @@ __global__ void __launch_bounds__(256) k_spmm(const SpmmArgs<T> a) {
 #pragma unroll
                 for (int r = 0; r < BR; ++r) {
                     T xv[V];
-                    VecIO<T, V>::ld(a.X + y0 + (size_t)r * k, xv);
+                    if (a.xzero) {
+#pragma unroll
+                        for (int v = 0; v < V; ++v) xv[v] = T(0);
+                    } else {
+                        VecIO<T, V>::ld(a.X + y0 + (size_t)r * k, xv);
+                    }
 #pragma unroll
                     for (int v = 0; v < V; ++v) xv[v] = xv[v] + a.omega * out[r][v];
                     VecIO<T, V>::st(a.Y + y0 + (size_t)r * k, xv);
@@ -245,7 +253,7 @@ __global__ void __launch_bounds__(256) k_spmm_generic(const SpmmArgs<T> a, int b
     const int64_t total = (int64_t)a.nbr * a.k;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int i = (int)(t / a.k), c = (int)(t % a.k);
-        const int k0 = a.row_ptr[i], k1 = a.row_ptr[i + 1];
+        const int k0 = a.row_ptr[i], k1 = (MODE == 1 && a.xzero) ? k0 : a.row_ptr[i + 1];
         T tv[64];
         for (int r = 0; r < br; ++r) {
             T s = 0;
@@ -266,7 +274,7 @@ __global__ void __launch_bounds__(256) k_spmm_generic(const SpmmArgs<T> a, int b
                 T s = 0;
                 for (int cc = 0; cc < br; ++cc) s = fma(a.Dinv[(size_t)i * br * br + r * br + cc], tv[cc], s);
                 const size_t o = ((size_t)i * br + r) * a.k + c;
-                a.Y[o] = a.X[o] + a.omega * s;
+                a.Y[o] = (a.xzero ? T(0) : a.X[o]) + a.omega * s;
             }
         }
     }
@@ -401,7 +409,7 @@ __global__ void __launch_bounds__(kMmaWarps * 32) k_spmm_mma(const SpmmArgs<floa
         for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
             for (int q = 0; q < 4; ++q) acc[nt][q] = 0.f;
-        const int k0 = a.row_ptr[i], k1 = a.row_ptr[i + 1];
+        const int k0 = a.row_ptr[i], k1 = (MODE == 1 && a.xzero) ? k0 : a.row_ptr[i + 1];
         if (k0 < k1) mma_prefetch<B>(a, k0, c0, st, 0, lane);
         cp_async_commit();
         for (int kk = k0; kk < k1; ++kk) {
@@ -481,7 +489,7 @@ __global__ void __launch_bounds__(kMmaWarps * 32) k_spmm_mma(const SpmmArgs<floa
                         const int row = g + 8 * h, col = c0 + nt * 8 + 2 * t + e;
                         if (row < B && col < k) {
                             const size_t idx = y0 + (size_t)row * k + col;
-                            a.Y[idx] = a.X[idx] + a.omega * acc[nt][2 * h + e];
+                            a.Y[idx] = (a.xzero ? 0.f : a.X[idx]) + a.omega * acc[nt][2 * h + e];
                         }
                     }
         }
@@ -1061,8 +1069,9 @@ static void ensure_batch(mgldg_mg* m, int k, const mgldg_bsr* A_outer) {
 }
 
 // ------------------------------------------------------- multi-RHS V-cycle
+// n Jacobi sweeps on level l; xzero: x is zero and not materialised
 template <class T>
-static void brelax(mgldg_mg* m, int l, int n) {
+static void brelax(mgldg_mg* m, int l, int n, bool xzero = false) {
     LevelData& L = m->L[l];
     BatchLevel& B = m->batch->L[l];
     mgldg_ctx* ctx = m->ctx;
@@ -1076,13 +1085,14 @@ static void brelax(mgldg_mg* m, int l, int n) {
         a.Dinv = BL<T>::D(L);
         a.B = BL<T>::b(B);
         a.omega = (T)m->p.omega;
+        a.xzero = (xzero && s == 0) ? 1 : 0;
         spmm_launch<T>(ctx, L.A->br, L.A->bc, a, 1, B.jac, MGLDG_K_JACOBI);
         std::swap(BL<T>::x(B), BL<T>::xt(B));
     }
 }
 
 template <class T>
-static void bcoarse(mgldg_mg* m, int l) {
+static void bcoarse(mgldg_mg* m, int l, bool xzero) {
     LevelData& L = m->L[l];
     BatchLevel& B = m->batch->L[l];
     mgldg_ctx* ctx = m->ctx;
@@ -1094,7 +1104,7 @@ static void bcoarse(mgldg_mg* m, int l) {
             k_bcoarse<T><<<k, 256, 0, ctx->stream>>>((int)L.n, k, BL<T>::b(B), BL<T>::x(B), nullptr, 1, 0);
         }
         check_launch();
-        brelax<T>(m, l, m->p.npre);
+        brelax<T>(m, l, m->p.npre, xzero);
         brelax<T>(m, l, m->p.npost);
         return;
     }
@@ -1107,17 +1117,17 @@ static void bcoarse(mgldg_mg* m, int l) {
 }
 
 template <class T>
-static void bvcycle(mgldg_mg* m, int l) {
+static void bvcycle(mgldg_mg* m, int l, bool xzero) {
     mgldg_ctx* ctx = m->ctx;
     if (l == (int)m->L.size() - 1) {
-        bcoarse<T>(m, l);
+        bcoarse<T>(m, l, xzero);
         return;
     }
     LevelData& L = m->L[l];
     BatchLevel& B = m->batch->L[l];
     BatchLevel& C = m->batch->L[l + 1];
     const int k = m->batch->k;
-    brelax<T>(m, l, m->p.npre);
+    brelax<T>(m, l, m->p.npre, xzero);
     ctx->cur_level = l;
     {
         // r = b - A x
@@ -1138,8 +1148,9 @@ static void bvcycle(mgldg_mg* m, int l) {
         a.Y = BL<T>::b(C);
         spmm_launch<T>(ctx, L.Tt->br, L.Tt->bc, a, 0, B.restrict_, MGLDG_K_TRANSFER);
     }
-    MG_CHECK_CUDA(cudaMemsetAsync(BL<T>::x(C), 0, m->L[l + 1].n * k * sizeof(T), ctx->stream));
-    bvcycle<T>(m, l + 1);
+    const bool czero = zero_start(m, l + 1);
+    if (!czero) MG_CHECK_CUDA(cudaMemsetAsync(BL<T>::x(C), 0, m->L[l + 1].n * k * sizeof(T), ctx->stream));
+    bvcycle<T>(m, l + 1, czero);
     ctx->cur_level = l;
     {
         // x += T x_c
@@ -1177,15 +1188,18 @@ static void bprecon(mgldg_mg* m, const double* R, double* S, bool x_is_zero) {
     } reset{ctx};
     if (m->p.precision != MGLDG_PREC_FP64) {
         bconvert<double, float>(ctx, nk, R, B.b32);
-        if (x_is_zero) MG_CHECK_CUDA(cudaMemsetAsync(B.x32, 0, nk * sizeof(float), ctx->stream));
-        else bconvert<double, float>(ctx, nk, S, B.x32);
-        bvcycle<float>(m, 0);
+        const bool z = x_is_zero && zero_start(m, 0);
+        if (x_is_zero && !z) MG_CHECK_CUDA(cudaMemsetAsync(B.x32, 0, nk * sizeof(float), ctx->stream));
+        else if (!x_is_zero) bconvert<double, float>(ctx, nk, S, B.x32);
+        bvcycle<float>(m, 0, z);
         bconvert<float, double>(ctx, nk, B.x32, S);
     } else {
         MG_CHECK_CUDA(cudaMemcpyAsync(B.b, R, nk * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-        if (x_is_zero) MG_CHECK_CUDA(cudaMemsetAsync(B.x, 0, nk * sizeof(double), ctx->stream));
-        else MG_CHECK_CUDA(cudaMemcpyAsync(B.x, S, nk * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-        bvcycle<double>(m, 0);
+        const bool z = x_is_zero && zero_start(m, 0);
+        if (x_is_zero && !z) MG_CHECK_CUDA(cudaMemsetAsync(B.x, 0, nk * sizeof(double), ctx->stream));
+        else if (!x_is_zero)
+            MG_CHECK_CUDA(cudaMemcpyAsync(B.x, S, nk * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+        bvcycle<double>(m, 0, z);
         MG_CHECK_CUDA(cudaMemcpyAsync(S, B.x, nk * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
     }
 }

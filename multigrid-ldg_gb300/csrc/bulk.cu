@@ -252,6 +252,10 @@ __global__ void __launch_bounds__(kRows * 32, Stage<VT>::kMinBlocks)
             if (JACOBI && (lane & 1) == 0) {
                 bi = __ldg(bvec + (size_t)row * kB + r);
                 if (!xzero) xi = __ldg(x + (size_t)row * kB + r);
+            } else if (!JACOBI && beta != 0.f && (lane & 1) == 0) {
+                // yin (it may be y itself: each entry is read and written
+                // by the same lane), issued before the product
+                bi = bvec[(size_t)row * kB + r];
             }
             const bool fits = s_fits[st] != 0;
             const VT* a = fits ? reinterpret_cast<const VT*>(sv) + (size_t)(k0 - kg) * kBlk : val + (size_t)k0 * kBlk;
@@ -284,7 +288,7 @@ __global__ void __launch_bounds__(kRows * 32, Stage<VT>::kMinBlocks)
                 if ((lane & 1) == 0) y[(size_t)row * kB + r] = xi + omega * yv;
             } else if ((lane & 1) == 0) {
                 float v = alpha * acc;
-                if (beta != 0.f) v += beta * bvec[(size_t)row * kB + r];
+                if (beta != 0.f) v += beta * bi;
                 y[(size_t)row * kB + r] = v;
             }
         }

@@ -134,7 +134,7 @@ static void relax(mgldg_mg* m, int i, int n, bool reverse, bool xzero = false) {
 // level but a directly solved coarsest one, with npre >= 1.  Gauss-Seidel
 // reads the old values of the rows after the current one, so its x stays
 // materialised.
-static bool zero_start(const mgldg_mg* m, int i) {
+bool zero_start(const mgldg_mg* m, int i) {
     if (m->p.relaxation != MGLDG_RELAX_JACOBI || m->p.npre < 1) return false;
     return i < (int)m->L.size() - 1 || m->p.solver == MGLDG_COARSE_RELAXATION;
 }

@@ -52,6 +52,9 @@ void mg_precon(mgldg_mg* m, const double* r, double* s);
 // the same with every launch issued directly (for capture into a graph)
 void mg_precon_eager(mgldg_mg* m, const double* r, double* s);
 void mg_take_errors(mgldg_mg* m);
+// true when level i's V-cycle starts from x = 0 with a Jacobi sweep that
+// reads neither x nor the operator, so x need not be zeroed (mg.cu)
+bool zero_start(const mgldg_mg* m, int i);
 
 struct PcgScalars {
     double delta_new, delta_old, delta0, alpha, beta, dq, rr, pad;
