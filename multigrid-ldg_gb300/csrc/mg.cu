@@ -25,6 +25,7 @@
 
 #include "api.cuh"
 #include "mg.cuh"
+#include "tail.cuh"
 #include "rowdot.cuh"
 
 using namespace mg;
@@ -174,6 +175,17 @@ static void vcycle(mgldg_mg* m, int i, bool xzero) {
     if (i == (int)m->L.size() - 1) {
         coarse_solve<T>(m, i, xzero);
         return;
+    }
+    if constexpr (std::is_same<T, float>::value) {
+        if (i == m->tail_start && xzero) {
+            // levels i .. last in one launch; the host's iterate buffers
+            // follow the sweeps' swaps as relax() would leave them
+            ctx->cur_level = i;
+            tail_launch(m, i, m->tail_count);
+            if ((m->p.npre + m->p.npost) & 1)
+                for (int l = i; l < (int)m->L.size() - 1; ++l) std::swap(m->L[l].x32, m->L[l].xt32);
+            return;
+        }
     }
     LevelData& L = m->L[i];
     LevelData& C = m->L[i + 1];
@@ -922,6 +934,7 @@ mgldg_mg::~mgldg_mg() {
     dfree(Cinv);
     dfree(r); dfree(d); dfree(q); dfree(s); dfree(hist); dfree(dhi); dfree(dlo);
     dfree(host_b); dfree(host_x);
+    dfree(tail_count);
     dfree(sc);
     if (h_sc) cudaFreeHost(h_sc);
     mg::batch_free(batch);
@@ -1065,6 +1078,23 @@ extern "C" int mgldg_mg_create(mgldg_ctx* ctx, const mgldg_ops* fine, const mgld
             m->Cinv = dalloc<double>((size_t)m->nc * m->nc);
             dense_spd_inverse(ctx, Ac, m->Cinv);
             phase("coarse", last);
+        }
+        // the coarse tail (opt-in): from the first level of at most
+        // MGLDG_VTAIL_ROWS block rows.  Off by default: on the 512^2 Q3
+        // solve it cut the event-timed coarse levels from 5.5 to 3.7 ms per
+        // solve, but the graph-replayed solve went from 53.2 to 54.5 ms --
+        // its ~28 grid barriers cost about what the replayed launches did.
+        {
+            const char* env = std::getenv("MGLDG_VTAIL_ROWS");
+            const long rows = env ? std::strtol(env, nullptr, 10) : 0;
+            for (int i = 1; rows > 0 && i < last; ++i)
+                if (m->L[i].ne <= rows) {
+                    if (tail_supported(m, i)) {
+                        m->tail_count = dalloc<unsigned>(1);
+                        m->tail_start = i;
+                    }
+                    break;
+                }
         }
         sync(ctx);
     } catch (...) {

@@ -108,6 +108,10 @@ struct mgldg_mg {
     // (stable addresses let the iteration graph be reused)
     double *host_b = nullptr, *host_x = nullptr;
     int64_t host_n = 0;
+    // the coarse end of the mixed Jacobi V-cycle as one launch (tail.cu):
+    // first level it covers (-1: none) and its barrier counter
+    int tail_start = -1;
+    unsigned* tail_count = nullptr;
     mg::Batch* batch = nullptr;   // multi-RHS work space (batched.cu)
     mg::SegWork* seg = nullptr;   // segmented-PCG work space (batched.cu)
     ~mgldg_mg();
