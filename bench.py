@@ -416,6 +416,24 @@ def run_batched(args, ctx, ext, torch, local, ws, precision=None):
     err0 = float(torch.linalg.norm(X[:, 0] - x1) / torch.linalg.norm(x1))
     nbr, _, br, _, nnzb = A.info()
     tiles = [mgldg.batch_tiles(mg, l) for l in range(mg.nlevels)]
+    # level-0 Jacobi SpMM of the profiled batch against HBM: per V-cycle
+    # npre + npost launches, the first from X = 0 (inverse diagonal blocks,
+    # B and X_out only), the others full sweeps (FP32 blocks, indices, B,
+    # X_in, X_out; k columns per vector)
+    nj, msj = ctx.prof_level(2, 0)
+    n0 = nbr * br
+    full = nnzb * br * br * 4 + nbr * br * br * 4 + 4 * nnzb + 4 * (nbr + 1) + 3 * n0 * k * 4
+    zero = nbr * br * br * 4 + 2 * n0 * k * 4
+    nsw = WL["npre"] + WL["npost"]
+    jbytes = ((nsw - 1) * full + zero) / nsw
+    hbm, peak_kind = peaks()
+    roof = None
+    if nj:
+        ach = jbytes * nj / (msj * 1e-3) / 1e9
+        roof = {"bound": "hbm", "kernel": "jacobi (multi-RHS SpMM, CUDA cores)" if prec != mgldg.PREC_MIXED_TF32
+                else "jacobi (multi-RHS SpMM, tensor cores 3xTF32)", "level": 0, "achieved": ach, "peak": hbm,
+                "unit": "GB/s", "frac": ach / hbm, "peak_kind": peak_kind, "launches": nj, "avg_launch_ms": msj / nj,
+                "algorithmic_bytes_per_launch": jbytes}
     out = {
         "workload": (f"{mesh}, Q2 LDG (9 DOF/element, {ndof:,} DOF), {k} right-hand sides "
                      f"(seeds 3001..{3000 + k}), RATRAT ({levels} levels, dense coarsest), "
@@ -431,6 +449,7 @@ def run_batched(args, ctx, ext, torch, local, ws, precision=None):
         "kernel_ms": {kk: round(v[1], 3) for kk, v in prof.items() if v[0]},
         "launches_per_batch": int(sum(v[0] for v in launches.values()) / steps),
         "outer_fp64_spmm_gflop": 2 * nnzb * br * br * k / 1e9,
+        "roofline": roof,
         "steps": steps,
     }
     del B, X, tmp, mg, prob
