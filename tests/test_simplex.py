@@ -131,6 +131,47 @@ def test_agglomeration_covers_and_coarsens():
     assert np.abs(T0 @ c - 1).max() <= 1e-8
 
 
+def test_external_agglomerator_graph_and_checks():
+    # the oracle hands an external agglomerator each level's dual graph
+    # (MGridGen's argument list) and rejects partitions that are out of
+    # range, leave an aggregate empty or report a bad count
+    _lib_or_skip()
+    p, t = mgldg.disk_mesh(0.2)
+    seen = []
+
+    def pairs(n, xadj, adjncy, adjwgt, vvol, vsurf, N, part):
+        seen.append((n, xadj.copy(), adjncy.copy(), adjwgt.copy(), vvol.copy(), vsurf.copy(), N))
+        part[:] = np.arange(n) // 2
+        return (n + 1) // 2
+
+    cb = O.set_agglomerator(pairs)
+    try:
+        pr = O.Problem.simplex(p, t, 2, 5.0, 5.0, agg_levels=2)
+    finally:
+        O.set_agglomerator(None)
+    del cb
+    n, xadj, adj, w, vol, surf, N = seen[0]
+    assert N == 2 and n == pr.ne and xadj[0] == 0 and len(adj) == xadj[-1] == 2 * (pr.nfaces - pr.nbfaces)
+    # symmetric weights, every element's volume, the disk's boundary measure
+    W = {(u, adj[k]): w[k] for u in range(n) for k in range(xadj[u], xadj[u + 1])}
+    assert all(abs(W[(v, u)] - wt) <= 1e-15 for (u, v), wt in W.items())
+    assert abs(vol.sum() - np.pi) < 0.2 and abs(surf.sum() - 2 * np.pi) < 0.1
+    assert np.array_equal(pr.partition(0), np.arange(pr.ne) // 2)
+    # the next level's graph sums the first level's pairs
+    assert seen[1][0] == (pr.ne + 1) // 2 and abs(seen[1][4].sum() - vol.sum()) <= 1e-12
+
+    for bad in (lambda n, part: (part.__setitem__(slice(None), n), n),         # out of range
+                lambda n, part: (part.__setitem__(slice(None), 0), 2),         # empty aggregate
+                lambda n, part: (part.__setitem__(slice(None), 0), 0)):        # bad count
+        cb = O.set_agglomerator(lambda n, xa, aj, aw, vv, vs, N, part, f=bad: f(n, part)[1])
+        try:
+            with pytest.raises(RuntimeError):
+                O.Problem.simplex(p, t, 2, 5.0, 5.0, agg_levels=2)
+        finally:
+            O.set_agglomerator(None)
+        del cb
+
+
 def test_ball_mesh_is_a_conforming_tetrahedralisation():
     _lib_or_skip()
     p, t = mgldg.ball_mesh(0.3)
