@@ -295,13 +295,21 @@ def run_config1(args, ctx, ext, torch, local, ws):
     e1.record(ext)
     e1.synchronize()
     ms = dist_max(e0.elapsed_time(e1) / nrep, ws)
-    bh = b.cpu().numpy()
-    xh = np.zeros_like(bh)
-    t0 = time.perf_counter()
+    # end to end through mgldg_pcg with pinned host b and x (x zeroed outside the clock)
+    bh = torch.empty(b.numel(), dtype=torch.float64, pin_memory=True)
+    bh.copy_(b.cpu())
+    xh = torch.zeros(b.numel(), dtype=torch.float64, pin_memory=True)
+    bh, xh = bh.numpy(), xh.numpy()
+    lib = mgldg.lib()
+    it_e2e = C.c_int()
+    hist_e2e = np.zeros(WL["maxit"])
+    e2e = 0.0
     for _ in range(nrep):
         xh[:] = 0.0
-        mgldg.pcg(ctx, A, bh, x=xh, precon=mg, tol=WL["tol"], maxit=WL["maxit"])
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / nrep
+        t0 = time.perf_counter()
+        ctx.check(lib.mgldg_pcg(ctx.h, mg.h, A.h, bh, xh, WL["tol"], WL["maxit"], C.byref(it_e2e), hist_e2e), "pcg")
+        e2e += time.perf_counter() - t0
+    e2e_ms = e2e * 1e3 / nrep
     out = {"workload": ("32x32 uniform quadtree, Q2 LDG (9,216 DOF), tau0=tauD=32, RATRAT 32->4 (4 levels, dense "
                         "coarsest, mean projection), FP64 block Gauss-Seidel omega=0.8 V(2,2), tol 1e-10"),
            "ms_per_solve": ms, "solves_per_s": 1e3 / ms, "e2e_ms_per_solve": e2e_ms, "iters": it.value}
@@ -892,18 +900,23 @@ def run_gpu(args, ws, rank, local):
     results[headline]["per_level_ms"] = {k: {str(l): round(v[1] / args.steps, 4) for l, v in d.items()}
                                          for k, d in per_level.items()}
 
-    # end to end through the public host API: pinned host b -> device, solve,
-    # x -> host, every step
+    # end to end through the C ABI's host-buffer call (mgldg_pcg, the
+    # reference's pcg(A, b, x, ...) with x in/out): pinned host b and x ->
+    # device, solve, x -> host, every step
     bpin = torch.empty(ndof, dtype=torch.float64, pin_memory=True)
     bpin.copy_(b.cpu())
     xpin = torch.zeros(ndof, dtype=torch.float64, pin_memory=True)
     bnp, xnp = bpin.numpy(), xpin.numpy()
+    lib = mgldg.lib()
+    it_e2e = C.c_int()
+    hist_e2e = np.zeros(WL["maxit"])
     e2e = []
     for k in range(args.warmup + args.steps):
         xnp[:] = 0.0
         dist_barrier(ws)
         t0 = time.perf_counter()
-        mgldg.pcg(ctx, A, bnp, x=xnp, precon=mgs[headline], tol=WL["tol"], maxit=WL["maxit"])
+        ctx.check(lib.mgldg_pcg(ctx.h, mgs[headline].h, A.h, bnp, xnp, WL["tol"], WL["maxit"], C.byref(it_e2e),
+                                hist_e2e), "pcg")
         dt = time.perf_counter() - t0
         if k >= args.warmup:
             e2e.append(dt * 1e3)
