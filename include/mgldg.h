@@ -280,6 +280,9 @@ int mgldg_problem_mesh_info(const mgldg_problem* pr, int* nfaces, int* nbfaces, 
  * unit disk with concentric rings of spacing 1/ceil(1/h), triangles in the
  * Morton order below, same calling pattern. */
 int mgldg_mesh_read(const char* path, int* np, int* nt, double* p, int* t);
+/* The same for Wireframe<N>, N = 2 (triangles) or 3 (tetrahedra: lines of
+ * x y z, then 1-based vertex quadruples); p[N*np], t[(N+1)*nt]. */
+int mgldg_mesh_read_nd(const char* path, int N, int* np, int* nt, double* p, int* t);
 int mgldg_disk_mesh(double h, int* np, int* nt, double* p, int* t);
 /* Reorders the N-simplices t[(N+1)*nt] in place, stably, by the Morton key
  * of their centroids (no reference counterpart).  Element order is block

@@ -1393,8 +1393,11 @@ extern "C" int mgldg_disk_mesh(double h, int* np, int* nt, double* p, int* t) {
 
 // Wireframe(file) (wireframe.h:24-67): "np nt", a header line, np lines of
 // coordinates, an empty line, nt lines of 1-based vertex indices
-extern "C" int mgldg_mesh_read(const char* path, int* np, int* nt, double* p, int* t) {
-    if (!path || !np || !nt) return MGLDG_ERR_ARG;
+// Wireframe<N>(file) (wireframe.h:24-67) for N = 2 (triangles) or 3
+// (tetrahedra): "np nt", one more header line, np lines of N coordinates,
+// an empty line, nt lines of N+1 one-based vertex indices.
+extern "C" int mgldg_mesh_read_nd(const char* path, int N, int* np, int* nt, double* p, int* t) {
+    if (!path || !np || !nt || (N != 2 && N != 3)) return MGLDG_ERR_ARG;
     std::ifstream ifs(path);
     if (!ifs.is_open()) return MGLDG_ERR_ARG;
     std::string line;
@@ -1408,40 +1411,42 @@ extern "C" int mgldg_mesh_read(const char* path, int* np, int* nt, double* p, in
     int ip = 0, it = 0;
     while (std::getline(ifs, line) && !line.empty()) {
         std::istringstream ss(line);
-        double v[2];
+        double v[3] = {0, 0, 0};
         int k = 0;
         double x;
-        while (ss >> x) {
-            if (k < 2) v[k] = x;
-            ++k;
-        }
-        if (k != 2 || ip >= n_p) return MGLDG_ERR_ARG;
-        if (p) {
-            p[2 * ip] = v[0];
-            p[2 * ip + 1] = v[1];
-        }
-        ++ip;
-    }
-    while (std::getline(ifs, line) && !line.empty()) {
-        std::istringstream ss(line);
-        int v[3];
-        int k = 0;
-        int x;
         while (ss >> x) {
             if (k < 3) v[k] = x;
             ++k;
         }
-        if (k != 3 || it >= n_t) return MGLDG_ERR_ARG;
-        for (int j = 0; j < 3; ++j)
+        if (k != N || ip >= n_p) return MGLDG_ERR_ARG;
+        if (p)
+            for (int d = 0; d < N; ++d) p[(size_t)N * ip + d] = v[d];
+        ++ip;
+    }
+    while (std::getline(ifs, line) && !line.empty()) {
+        std::istringstream ss(line);
+        int v[4] = {0, 0, 0, 0};
+        int k = 0;
+        int x;
+        while (ss >> x) {
+            if (k < 4) v[k] = x;
+            ++k;
+        }
+        if (k != N + 1 || it >= n_t) return MGLDG_ERR_ARG;
+        for (int j = 0; j <= N; ++j)
             if (v[j] < 1 || v[j] > n_p) return MGLDG_ERR_ARG;
         if (t)
-            for (int j = 0; j < 3; ++j) t[3 * it + j] = v[j] - 1;
+            for (int j = 0; j <= N; ++j) t[(size_t)(N + 1) * it + j] = v[j] - 1;
         ++it;
     }
     if (ip != n_p || it != n_t) return MGLDG_ERR_SHAPE;
     *np = n_p;
     *nt = n_t;
     return MGLDG_OK;
+}
+
+extern "C" int mgldg_mesh_read(const char* path, int* np, int* nt, double* p, int* t) {
+    return mgldg_mesh_read_nd(path, 2, np, nt, p, t);
 }
 
 extern "C" int mgldg_simplex_problem_create_nd(mgldg_ctx* ctx, int N, int np, const double* p, int nt, const int* t,

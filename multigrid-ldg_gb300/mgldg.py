@@ -41,7 +41,7 @@ EXPORTS = [
     "mgldg_bsr_mm_dev", "mgldg_mg_vcycle_batched_dev", "mgldg_pcg_batched_dev", "mgldg_pcg_batched",
     "mgldg_mg_batch_tiles", "mgldg_quadtree_create", "mgldg_quadtree_destroy", "mgldg_quadtree_info",
     "mgldg_quadtree_layer", "mgldg_h_points", "mgldg_seeded_points", "mgldg_quadtree_problem_create",
-    "mgldg_problem_mesh_info", "mgldg_mesh_read", "mgldg_disk_mesh", "mgldg_mesh_morton_order", "mgldg_simplex_problem_create",
+    "mgldg_problem_mesh_info", "mgldg_mesh_read", "mgldg_mesh_read_nd", "mgldg_disk_mesh", "mgldg_mesh_morton_order", "mgldg_simplex_problem_create",
     "mgldg_problem_partition", "mgldg_simplex_master", "mgldg_pcg_segmented_dev",
     "mgldg_simplex_problem_create_nd", "mgldg_ball_mesh", "mgldg_simplex_master_nd", "mgldg_bsr_clone",
 ]
@@ -177,6 +177,7 @@ def lib():
         L.mgldg_quadtree_problem_create.argtypes = [vp, vp, C.c_int, C.c_double, C.c_double, C.c_int, pvp]
         L.mgldg_problem_mesh_info.argtypes = [vp, ip, ip, ip]
         L.mgldg_mesh_read.argtypes = [C.c_char_p, ip, ip, vp, vp]
+        L.mgldg_mesh_read_nd.argtypes = [C.c_char_p, C.c_int, ip, ip, vp, vp]
         L.mgldg_disk_mesh.argtypes = [C.c_double, ip, ip, vp, vp]
         L.mgldg_simplex_problem_create.argtypes = [vp, C.c_int, _dp, C.c_int, _ip, C.c_int, C.c_double, C.c_double,
                                                    C.c_int, C.c_uint64, pvp]
@@ -629,9 +630,11 @@ def ball_mesh(h):
     return _two_call(lib().mgldg_ball_mesh, C.c_double(h), N=3)
 
 
-def read_mesh(path):
-    """The reference's .mesh wireframe: (points[np,2], triangles[nt,3], 0-based)."""
-    return _two_call(lib().mgldg_mesh_read, str(path).encode())
+def read_mesh(path, N=2):
+    """The reference's .mesh wireframe (Wireframe<N>): (points[np,N], simplices[nt,N+1], 0-based)."""
+    if N == 2:
+        return _two_call(lib().mgldg_mesh_read, str(path).encode())
+    return _two_call(lib().mgldg_mesh_read_nd, str(path).encode(), N, N=N)
 
 
 def mesh_union(meshes):
