@@ -78,6 +78,21 @@ int mgldg_bsr_create(mgldg_ctx* ctx, int nbr, int nbc, int br, int bc,
                      const int* row_ptr, const int* col_idx, const double* vals,
                      mgldg_bsr** A);
 int mgldg_bsr_destroy(mgldg_bsr* A);
+/* Incremental host-side assembly with the reference's block calls, for
+ * callers that build a matrix block by block: create = reset(m, n)
+ * (sparseblockmatrix.tpp:120-127), set = setBlock (:79-84, overwrites),
+ * add = addToBlock (:93-100, sums in call order), exists = blockExists,
+ * nnzb.  export writes the sorted block-CSR (pass NULL arrays to skip);
+ * finalize uploads it as a device BSR. */
+typedef struct mgldg_bsr_builder mgldg_bsr_builder;
+int mgldg_bsr_builder_create(int nbr, int nbc, int br, int bc, mgldg_bsr_builder** out);
+int mgldg_bsr_builder_set(mgldg_bsr_builder* b, int i, int j, const double* block);
+int mgldg_bsr_builder_add(mgldg_bsr_builder* b, int i, int j, const double* block);
+int mgldg_bsr_builder_exists(const mgldg_bsr_builder* b, int i, int j, int* exists);
+int mgldg_bsr_builder_nnzb(const mgldg_bsr_builder* b, int64_t* nnzb);
+int mgldg_bsr_builder_export(const mgldg_bsr_builder* b, int* row_ptr, int* col_idx, double* vals);
+int mgldg_bsr_builder_finalize(mgldg_ctx* ctx, const mgldg_bsr_builder* b, mgldg_bsr** A);
+int mgldg_bsr_builder_destroy(mgldg_bsr_builder* b);
 /* A device-side copy of A (pattern and values), owned by the caller. */
 int mgldg_bsr_clone(mgldg_ctx* ctx, const mgldg_bsr* A, mgldg_bsr** out);
 /* blockRows/blockCols/rowsPerBlock/colsPerBlock/nnzb (sparseblockmatrix.h:82-110) */

@@ -44,6 +44,8 @@ EXPORTS = [
     "mgldg_problem_mesh_info", "mgldg_mesh_read", "mgldg_mesh_read_nd", "mgldg_disk_mesh", "mgldg_mesh_morton_order", "mgldg_simplex_problem_create",
     "mgldg_problem_partition", "mgldg_simplex_master", "mgldg_pcg_segmented_dev",
     "mgldg_simplex_problem_create_nd", "mgldg_ball_mesh", "mgldg_simplex_master_nd", "mgldg_bsr_clone",
+    "mgldg_bsr_builder_create", "mgldg_bsr_builder_set", "mgldg_bsr_builder_add", "mgldg_bsr_builder_exists",
+    "mgldg_bsr_builder_nnzb", "mgldg_bsr_builder_export", "mgldg_bsr_builder_finalize", "mgldg_bsr_builder_destroy",
 ]
 
 
@@ -116,6 +118,14 @@ def lib():
         L.mgldg_master_tables.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         L.mgldg_bsr_create.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, _ip, _ip, _dp, pvp]
         L.mgldg_bsr_destroy.argtypes = [vp]
+        L.mgldg_bsr_builder_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, pvp]
+        L.mgldg_bsr_builder_set.argtypes = [vp, C.c_int, C.c_int, _dp]
+        L.mgldg_bsr_builder_add.argtypes = [vp, C.c_int, C.c_int, _dp]
+        L.mgldg_bsr_builder_exists.argtypes = [vp, C.c_int, C.c_int, ip]
+        L.mgldg_bsr_builder_nnzb.argtypes = [vp, i64p]
+        L.mgldg_bsr_builder_export.argtypes = [vp, vp, vp, vp]
+        L.mgldg_bsr_builder_finalize.argtypes = [vp, vp, pvp]
+        L.mgldg_bsr_builder_destroy.argtypes = [vp]
         L.mgldg_bsr_clone.argtypes = [vp, vp, pvp]
         L.mgldg_bsr_info.argtypes = [vp, ip, ip, ip, ip, i64p]
         L.mgldg_bsr_download.argtypes = [vp, vp, _ip, _ip, _dp]
@@ -256,6 +266,72 @@ class Context:
             self.close()
         except Exception:
             pass
+
+
+class BlockBuilder:
+    """Host-side block assembly with the reference's calls: reset (the
+    constructor), setBlock, addToBlock, blockExists, nnzb; export() gives the
+    sorted block-CSR, finalize(ctx) the GPU SparseBlockMatrix."""
+
+    def __init__(self, nbr, nbc, br, bc):
+        self.shape = (nbr, nbc, br, bc)
+        self.h = C.c_void_p()
+        rc = lib().mgldg_bsr_builder_create(nbr, nbc, br, bc, C.byref(self.h))
+        if rc:
+            raise MgldgError(rc, "bsr_builder_create")
+
+    def _block(self, block):
+        b = np.ascontiguousarray(block, dtype=np.float64).reshape(-1)
+        if b.size != self.shape[2] * self.shape[3]:
+            raise ValueError("block has the wrong size")
+        return b
+
+    def set_block(self, i, j, block):
+        rc = lib().mgldg_bsr_builder_set(self.h, i, j, self._block(block))
+        if rc:
+            raise MgldgError(rc, "bsr_builder_set")
+
+    def add_to_block(self, i, j, block):
+        rc = lib().mgldg_bsr_builder_add(self.h, i, j, self._block(block))
+        if rc:
+            raise MgldgError(rc, "bsr_builder_add")
+
+    def block_exists(self, i, j):
+        e = C.c_int()
+        rc = lib().mgldg_bsr_builder_exists(self.h, i, j, C.byref(e))
+        if rc:
+            raise MgldgError(rc, "bsr_builder_exists")
+        return bool(e.value)
+
+    def nnzb(self):
+        n = C.c_int64()
+        lib().mgldg_bsr_builder_nnzb(self.h, C.byref(n))
+        return n.value
+
+    def export(self):
+        nbr, _, br, bc = self.shape
+        n = self.nnzb()
+        rp = np.zeros(nbr + 1, np.int32)
+        ci = np.zeros(max(1, n), np.int32)
+        v = np.zeros(max(1, n) * br * bc)
+        rc = lib().mgldg_bsr_builder_export(self.h, rp.ctypes.data_as(C.c_void_p), ci.ctypes.data_as(C.c_void_p),
+                                            v.ctypes.data_as(C.c_void_p))
+        if rc:
+            raise MgldgError(rc, "bsr_builder_export")
+        return rp, ci[:n], v[:n * br * bc].reshape(n, br, bc)
+
+    def finalize(self, ctx):
+        h = C.c_void_p()
+        ctx.check(lib().mgldg_bsr_builder_finalize(ctx.h, self.h, C.byref(h)), "bsr_builder_finalize")
+        return SparseBlockMatrix(ctx, h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            try:
+                lib().mgldg_bsr_builder_destroy(self.h)
+            except Exception:
+                pass
+            self.h = None
 
 
 class SparseBlockMatrix:
