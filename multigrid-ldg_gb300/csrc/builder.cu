@@ -25,10 +25,16 @@ int put(mgldg_bsr_builder* b, int i, int j, const double* block, bool add) {
         const size_t bs = b->bs();
         auto it = b->where.find(b->key(i, j));
         if (it == b->where.end()) {
-            b->where.emplace(b->key(i, j), (int64_t)b->bi.size());
+            // grow every array before indexing the new block, so a failed
+            // allocation leaves the builder as it was
+            const size_t nb = b->bi.size();
+            b->vals.reserve(b->vals.size() + bs);
+            b->bi.reserve(nb + 1);
+            b->bj.reserve(nb + 1);
+            b->where.emplace(b->key(i, j), (int64_t)nb);
+            b->vals.insert(b->vals.end(), block, block + bs);
             b->bi.push_back(i);
             b->bj.push_back(j);
-            b->vals.insert(b->vals.end(), block, block + bs);
             return MGLDG_OK;
         }
         double* dst = b->vals.data() + (size_t)it->second * bs;
